@@ -1,0 +1,222 @@
+// Device-side helpers: per-degree launch configuration, constant basis tables
+// and the column-wise sum-factorisation primitives shared by every operator
+// kernel.
+//
+// Thread layout of the operator kernels ("column" layout): a block holds CPB
+// cells; each cell is served by NQ = 2k+1 threads.  Thread `col` owns the
+// quadrature column x = x_col of its cell: it evaluates every field on the
+// NQ points of that column in registers (x-contraction from the cell's dof
+// tile in shared memory, then the z-contraction in registers), does the
+// point-wise physics, and contracts the submitted values back along z.  The
+// final x-contraction and the face terms need one exchange through shared
+// memory.  The same thread also serves face quadrature point `col` of each
+// of the cell's four faces.  Face terms are element-centric: each cell reads
+// the neighbour's face trace and adds only its own side, so no atomics are
+// needed and results are bitwise reproducible run to run.
+#pragma once
+#include "atm_internal.h"
+
+namespace atm {
+
+template <int K>
+struct Cfg {
+  static constexpr int NN = K + 1;
+  static constexpr int NQ = 2 * K + 1;
+  static constexpr int NN2 = NN * NN;
+  static constexpr int NQ2 = NQ * NQ;
+  static constexpr int CPB = 128 / NQ;  // cells per block
+  static constexpr int THREADS = CPB * NQ;
+};
+
+// [degree][0: values, 1: derivatives][q*(k+1)+i] at the 2k+1 Gauss points.
+// Each translation unit holds its own copy in its constant bank.
+static __constant__ double c_basis[KMAX + 1][2][NQ_MAX * NN_MAX];
+
+static inline int upload_basis_here(const double *table) {
+  return cudaMemcpyToSymbol(c_basis, table, sizeof(c_basis)) == cudaSuccess ? 0 : 1;
+}
+
+template <int K>
+__device__ __forceinline__ double bS(int q, int i) { return c_basis[K][0][q * (K + 1) + i]; }
+template <int K>
+__device__ __forceinline__ double bD(int q, int i) { return c_basis[K][1][q * (K + 1) + i]; }
+
+struct SrcPtrs {
+  const double *p[12];
+};
+
+// local node index of node i (0..k) on face f: 0 x=0, 1 x=1, 2 z=0, 3 z=1
+template <int K>
+__device__ __forceinline__ int face_node(int f, int i) {
+  constexpr int NN = K + 1;
+  return f == 0 ? i * NN : (f == 1 ? i * NN + K : (f == 2 ? i : K * NN + i));
+}
+
+// thread-dependent basis row (x = x_col) and column (node t) in registers
+template <int K>
+__device__ __forceinline__ void load_rows(int col, double (&Sx)[K + 1], double (&Dx)[K + 1]) {
+#pragma unroll
+  for (int i = 0; i <= K; ++i) {
+    Sx[i] = bS<K>(col, i);
+    Dx[i] = bD<K>(col, i);
+  }
+}
+template <int K>
+__device__ __forceinline__ void load_cols(int t, double (&St)[2 * K + 1],
+                                          double (&Dt)[2 * K + 1]) {
+#pragma unroll
+  for (int q = 0; q < 2 * K + 1; ++q) {
+    St[q] = bS<K>(q, t);
+    Dt[q] = bD<K>(q, t);
+  }
+}
+
+// values of a nodal tile on the thread's quadrature column
+template <int K>
+__device__ __forceinline__ void eval_col(const double *__restrict__ tile,
+                                         const double (&Sx)[K + 1], double (&v)[2 * K + 1]) {
+  constexpr int NN = K + 1, NQ = 2 * K + 1;
+  double t[NN];
+#pragma unroll
+  for (int iz = 0; iz < NN; ++iz) {
+    double s = 0.0;
+#pragma unroll
+    for (int ix = 0; ix < NN; ++ix) s = fma(Sx[ix], tile[iz * NN + ix], s);
+    t[iz] = s;
+  }
+#pragma unroll
+  for (int qz = 0; qz < NQ; ++qz) {
+    double s = 0.0;
+#pragma unroll
+    for (int iz = 0; iz < NN; ++iz) s = fma(bS<K>(qz, iz), t[iz], s);
+    v[qz] = s;
+  }
+}
+
+// z-contraction of the submitted quantities of one column:
+//   xa[iz][col] = sum_qz S(qz,iz) V + D(qz,iz) Geta ;  xb[iz][col] = sum_qz S(qz,iz) Gxi
+// V, Gxi, Geta already carry JxW and the inverse Jacobian.
+template <int K, bool HAS_V, bool HAS_G>
+__device__ __forceinline__ void integrate_col_z(const double (&V)[2 * K + 1],
+                                                const double (&Gxi)[2 * K + 1],
+                                                const double (&Get)[2 * K + 1],
+                                                double *__restrict__ xa,
+                                                double *__restrict__ xb, int col) {
+  constexpr int NN = K + 1, NQ = 2 * K + 1;
+#pragma unroll
+  for (int iz = 0; iz < NN; ++iz) {
+    double sa = 0.0, sb = 0.0;
+#pragma unroll
+    for (int qz = 0; qz < NQ; ++qz) {
+      if (HAS_V) sa = fma(bS<K>(qz, iz), V[qz], sa);
+      if (HAS_G) {
+        sa = fma(bD<K>(qz, iz), Get[qz], sa);
+        sb = fma(bS<K>(qz, iz), Gxi[qz], sb);
+      }
+    }
+    xa[iz * NQ + col] = sa;
+    if (HAS_G) xb[iz * NQ + col] = sb;
+  }
+}
+
+// x-contraction for output node column ix = t: out[iz] = sum_qx S(qx,t) xa + D(qx,t) xb
+template <int K, bool HAS_G>
+__device__ __forceinline__ void integrate_out(const double *__restrict__ xa,
+                                              const double *__restrict__ xb,
+                                              const double (&St)[2 * K + 1],
+                                              const double (&Dt)[2 * K + 1],
+                                              double (&out)[K + 1]) {
+  constexpr int NN = K + 1, NQ = 2 * K + 1;
+#pragma unroll
+  for (int iz = 0; iz < NN; ++iz) {
+    double s = 0.0;
+#pragma unroll
+    for (int qx = 0; qx < NQ; ++qx) {
+      s = fma(St[qx], xa[iz * NQ + qx], s);
+      if (HAS_G) s = fma(Dt[qx], xb[iz * NQ + qx], s);
+    }
+    out[iz] = s;
+  }
+}
+
+// add the face contributions F[f][q] (JxW included) to output node column t
+template <int K>
+__device__ __forceinline__ void add_face_out(const double *__restrict__ F, int t,
+                                             const double (&St)[2 * K + 1],
+                                             double (&out)[K + 1]) {
+  constexpr int NN = K + 1, NQ = 2 * K + 1;
+  // faces z=0 / z=1: node (iz=0|K, ix=t)
+  double s2 = 0.0, s3 = 0.0;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    s2 = fma(St[q], F[2 * NQ + q], s2);
+    s3 = fma(St[q], F[3 * NQ + q], s3);
+  }
+  out[0] += s2;
+  out[K] += s3;
+  // faces x=0 / x=1: whole node column ix = 0 / ix = K
+  if (t == 0 || t == K) {
+    const double *Ff = F + (t == 0 ? 0 : NQ);
+#pragma unroll
+    for (int iz = 0; iz < NN; ++iz) {
+      double s = 0.0;
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) s = fma(bS<K>(q, iz), Ff[q], s);
+      out[iz] += s;
+    }
+  }
+}
+
+// trace of a nodal tile at face quadrature point `col` (row Sx = S[col][.])
+template <int K>
+__device__ __forceinline__ double face_val(const double *__restrict__ tile, int f,
+                                           const double (&Sx)[K + 1]) {
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i <= K; ++i) s = fma(Sx[i], tile[face_node<K>(f, i)], s);
+  return s;
+}
+
+// cooperative, coalesced copy of the block's cells of one field into tiles
+// dst tile slot = tiles[(lc*NT + t0 + comp)*NN2 + i]
+template <int K>
+__device__ __forceinline__ void load_tiles(double *__restrict__ tiles, int NT, int t0,
+                                           const double *__restrict__ src, int ncomp,
+                                           int c0, int cnt) {
+  constexpr int NN2 = (K + 1) * (K + 1);
+  const int per = ncomp * NN2;
+  const double *s = src + (long)c0 * per;
+  for (int e = threadIdx.x; e < cnt * per; e += blockDim.x) {
+    const int lc = e / per;
+    const int r = e - lc * per;
+    const int comp = r / NN2;
+    const int i = r - comp * NN2;
+    tiles[(lc * NT + t0 + comp) * NN2 + i] = s[e];
+  }
+}
+
+// physical gradient (gx, gz) at a quadrature point -> reference space * JxW
+struct QGeo {
+  double xx, xz, ex, ez, jxw;
+};
+template <int K>
+__device__ __forceinline__ QGeo qgeo(const double *__restrict__ g, int q) {
+  constexpr int NQ2 = (2 * K + 1) * (2 * K + 1);
+  QGeo r;
+  r.xx = g[q];
+  r.xz = g[NQ2 + q];
+  r.ex = g[2 * NQ2 + q];
+  r.ez = g[3 * NQ2 + q];
+  r.jxw = g[4 * NQ2 + q];
+  return r;
+}
+
+template <int K>
+inline size_t smem_bytes(int n_tiles, int ncomp_out) {
+  using C = Cfg<K>;
+  return sizeof(double) * (size_t)C::CPB *
+         ((size_t)n_tiles * C::NN2 + (size_t)ncomp_out * 2 * C::NN * C::NQ +
+          (size_t)ncomp_out * 4 * C::NQ);
+}
+
+}  // namespace atm

@@ -1,0 +1,247 @@
+// Internal declarations shared by the host and device translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/atm_gb300.h"
+
+namespace atm {
+
+constexpr int KMAX = 5;           // highest supported polynomial degree
+constexpr int NQ_MAX = 2 * KMAX + 1;
+constexpr int NN_MAX = KMAX + 1;
+constexpr double GAS_GAMMA = 1.4;  // EquationData::Cp_Cv (equation_data.h:23)
+
+// IMEX ARK2 tableau, euler_operator.h:220-240
+struct Tableau {
+  double gamma, a21, a22, a31, a32, a33;
+  double a21t, a22t, a31t, a32t, a33t, b1, b2, b3;
+  static Tableau make();
+};
+
+// Per-stage weights handed to the explicit-operator kernels.
+struct Solver;
+
+struct StageCoef {
+  double ca[3];  // explicit advection weights (a / b)
+  double ct[3];  // pressure / enthalpy weights (a~ / b)
+  double cg[3];  // gravity weights (a~ / b)
+  double dt, Ma, Fr;
+};
+
+
+// Kernel families timed by the optional per-launch CUDA-event timers.
+enum KFam {
+  KF_RHS_RHO = 0, KF_RHS_VEL, KF_RHS_PRES, KF_B, KF_CD, KF_MASS, KF_DIAG, KF_BLOCK_INV,
+  KF_BLOCK_APPLY, KF_COUNT
+};
+
+// CUDA-event timers around operator launches (off unless enabled).
+struct KTimer {
+  bool on = false;
+  std::vector<cudaEvent_t> ev;  // pairs (start, stop)
+  std::vector<int> fam;         // family of each pair
+  size_t used = 0;              // pairs recorded since the last read
+  std::vector<double> bytes, flops;  // algorithmic bytes / FP64 flops per pair
+  double ms[KF_COUNT] = {0};
+  long n[KF_COUNT] = {0};
+  double tb[KF_COUNT] = {0}, tf[KF_COUNT] = {0};
+};
+
+// Every kernel launch of the library increments this counter.
+extern std::atomic<long> g_kernel_launches;
+
+// Device geometry + connectivity of one mesh.
+struct Mesh {
+  int nc = 0, k = 0, nn = 0, nq = 0, nn2 = 0, nq2 = 0;
+  double *qgeo = nullptr;  // [nc][5][nq2]: dxi/dx*JxW, dxi/dz*JxW, deta/dx*JxW, deta/dz*JxW, JxW
+  double *fgeo = nullptr;  // [nc][4][3][nq]: n_x, n_z, JxW (own-side, outward)
+  int *nbr = nullptr;      // [nc][4] neighbour cell, -1 at a wall
+  int *nbrf = nullptr;     // [nc][4] neighbour's local face index
+  double *minv = nullptr;  // [nc][nn2*nn2] inverse unit mass, stored transposed
+};
+
+}  // namespace atm
+
+struct atm_ctx {
+  int device = 0;
+  int k = 0, nn = 0, nq = 0, nn2 = 0, nq2 = 0, nc = 0, mapdeg = 0;
+  cudaStream_t stream = nullptr;
+  atm::Mesh mesh;
+  double dt = 1.0, Ma = 1.0, Fr = 1.0;
+  int hstage = 1, nsstage = 1;
+  atm::Tableau tab;
+  // frozen fields (owned copies) and derived data
+  double *rho_fix = nullptr, *pres_fix = nullptr, *u_fix = nullptr;
+  double *ainv = nullptr;       // [nc][nn2*nn2] inverse of rho_fix-weighted mass
+  double *invdiag_D = nullptr;  // inverse diagonal of D (Schur Jacobi)
+  // workspace
+  double *wv1 = nullptr, *wv2 = nullptr;  // velocity-sized
+  double *ws1 = nullptr, *ws2 = nullptr;  // scalar-sized
+  double *red = nullptr;                  // reduction partials (device)
+  double *red_out = nullptr;              // reduction results (device)
+  double *h_red = nullptr;                // pinned host mirror of red_out
+  // GMRES basis (restart+1 scalar vectors) + small device arrays
+  int restart = 28;
+  double *krylov = nullptr;
+  double *dsmall = nullptr;  // device scratch for Hessenberg columns / y
+  atm::Solver *solver = nullptr;
+  mutable atm::KTimer timer;
+  long n_scalar() const { return (long)nc * nn2; }
+  long n_vector() const { return 2L * nc * nn2; }
+};
+
+namespace atm {
+
+// ------------------------------------------------------------------ errors --
+void set_error(const std::string &msg);
+int cuda_fail(cudaError_t e, const char *where);
+#define ATM_CUDA(call)                                        \
+  do {                                                        \
+    cudaError_t _e = (call);                                  \
+    if (_e != cudaSuccess) return atm::cuda_fail(_e, #call);  \
+  } while (0)
+#define ATM_CHECK_LAUNCH(where)                       \
+  do {                                                \
+    atm::g_kernel_launches.fetch_add(1);              \
+    ATM_CUDA(cudaGetLastError());                     \
+  } while (0)
+
+// RAII: records a (start, stop) event pair around the launches in scope
+struct TimedRegion {
+  const atm_ctx &c;
+  size_t slot;
+  bool on;
+  // bytes: algorithmic HBM bytes of the launch (fields read + written, 8 B
+  // per node value); flops: FP64 flops of its sum-factorisation contractions
+  TimedRegion(const atm_ctx &ctx, int family, double bytes = 0.0, double flops = 0.0);
+  ~TimedRegion();
+};
+
+// ------------------------------------------------------------------ basis --
+// Host tables: S[q*nn+i] = l_i(x_q), D[q*nn+i] = l_i'(x_q) on Gauss points.
+struct HostBasis {
+  int k, nn, nq;
+  std::vector<double> gll, gauss, weights, S, D;
+};
+HostBasis make_basis(int k);
+std::vector<double> gll_nodes(int k);
+void lagrange_eval(const std::vector<double> &nodes, double x, double *val, double *der);
+// upload S/D tables of every degree to each translation unit's constant bank
+int upload_basis_all();
+
+// --------------------------------------------------------- kernel launches --
+// every launcher returns ATM_OK or an error status, and runs on `st`
+int launch_rhs_rho(const atm_ctx &c, int stage, double *dst, const double *const *src,
+                   const StageCoef &co);
+int launch_rhs_vel(const atm_ctx &c, int stage, double *dst, const double *const *src,
+                   const StageCoef &co);
+int launch_rhs_pres(const atm_ctx &c, int stage, double *dst, const double *const *src,
+                    const StageCoef &co);
+// B p -> dst (velocity); mode 0: dst = B p; 1: dst -= B p;
+// 2: dst = A^{-1} B p (uses c.ainv)
+int launch_B(const atm_ctx &c, double *dst, const double *p, double coeff, int mode);
+// C/D family on pressure space:
+//   mode 0: dst = C w
+//   mode 1: dst = sD*D p - C w
+//   mode 2: dst = invdiag .* (sD*D p - C w)
+//   mode 3: dst -= C w
+int launch_CD(const atm_ctx &c, double *dst, const double *w, const double *p,
+              const double *pfix, double coeff, int mode);
+// matrix-free mass apply: dst = M_w src, weight = tile field or constant scale
+int launch_mass(const atm_ctx &c, double *dst, const double *src, int ncomp,
+                const double *weight, double scale);
+// inverse diagonal of the (weighted) mass: out for ncomp components
+int launch_inv_diag(const atm_ctx &c, double *out, int ncomp, const double *weight,
+                    double scale);
+// build per-cell inverse of the weighted mass (weight null -> unit), transposed
+int launch_block_inverse(const atm_ctx &c, double *out, const double *weight);
+// dst = scale * Binv src, ncomp components per cell
+int launch_block_apply(const atm_ctx &c, double *dst, const double *src, const double *binv,
+                       int ncomp, double scale);
+
+// ----------------------------------------------------------- vector ops ---
+// All run on `st`, deterministic two-pass reductions.
+int vec_copy(cudaStream_t st, double *dst, const double *src, long n);
+int vec_fill(cudaStream_t st, double *dst, double v, long n);
+int vec_axpy(cudaStream_t st, double *y, double a, const double *x, long n);  // y += a x
+int vec_xmy_scaled(cudaStream_t st, double *dst, const double *d, const double *b,
+                   const double *t, long n);  // dst = d .* (b - t)
+int vec_scale_by_inv_norm(cudaStream_t st, double *dst, const double *src,
+                          const double *normsq, long n);  // dst = src/sqrt(*normsq)
+// partial-sum buffer `red` must hold 29*RED_BLOCKS doubles
+constexpr int RED_BLOCKS = 608;
+int vec_dot(cudaStream_t st, const double *x, const double *y, long n, double *red,
+            double *out);  // out[0] = x.y (device)
+int vec_multidot(cudaStream_t st, const double *V, long ldv, int m, const double *w, long n,
+                 double *red, double *out);  // out[l] = V_l . w, l < m
+// w += sign * sum_l h[l] V_l  (h device)
+int vec_multiaxpy(cudaStream_t st, double *w, const double *V, long ldv, int m,
+                  const double *h, double sign, long n);
+// out[0] = max|a-b|, out[1] = max|a| (b may be null -> out[0] = out[1])
+int vec_maxdiff(cudaStream_t st, const double *a, const double *b, long n, double *red,
+                double *out);
+// out[0..3] = min rho, max |rho|, max sqrt(g p/rho), max |u|
+int vec_diagnostics(cudaStream_t st, const double *rho, const double *u, const double *p,
+                    int nc, int nn2, double *red, double *out);
+int vec_sponge(cudaStream_t st, double *u, const double *alpha, double dt, double ub0,
+               double ub1, int nc, int nn2);
+
+// ------------------------------------------------------------ mesh set-up --
+int mesh_upload(atm_ctx &c, int mapdeg, const double *nodes, int n_inner, const int *inner,
+                int n_bdry, const int *bdry);
+void mesh_free(Mesh &m);
+
+// ---------------------------------------------------------- operator glue --
+// FP64 flops of the sum-factorisation contractions per cell (2 per FMA)
+inline double fl_eval(int k) {  // values of one field at the Gauss points
+  const double nn = k + 1, nq = 2 * k + 1;
+  return 2.0 * (nq * nn * nn + nq * nq * nn);
+}
+inline double fl_integrate(int k, bool grad) {  // one output component
+  const double nn = k + 1, nq = 2 * k + 1;
+  return grad ? 2.0 * (3 * nn * nq * nq + 2 * nn * nn * nq) : 2.0 * (nn * nq * nq + nn * nn * nq);
+}
+inline double fl_face(int k) {  // one field trace at the points of one face
+  return 2.0 * (2 * k + 1) * (k + 1);
+}
+StageCoef stage_coef_rho(const atm_ctx &c, int stage);
+StageCoef stage_coef_flux(const atm_ctx &c, int stage);
+double implicit_coeff(const atm_ctx &c);
+int schur_apply(atm_ctx &c, double *dst, const double *p, bool precondition);
+int op_vmult(atm_ctx &c, double *dst, const double *src);
+int op_solve(atm_ctx &c, double *x, const double *b, double tol, int maxit, int *its,
+             double *res);
+int gmres_schur(atm_ctx &c, double *x, const double *b, double tol, int maxit, int *its,
+                double *res);
+int read_scalars(atm_ctx &c, int n);  // device red_out[0..n) -> h_red (sync)
+int rebuild_ainv(atm_ctx &c);
+
+// ------------------------------------------------------------ time loop --
+struct Solver {
+  double eps = 1e-8;
+  int max_its = 30000;
+  int precision = 0;
+  double time = 0.0;
+  long steps = 0, picard_total = 0, krylov_total = 0, failures = 0;
+  int last_picard[2] = {0, 0};
+  double ubg0 = 0.0, ubg1 = 0.0;
+  bool sponge = false;
+  // state and stage vectors (device)
+  double *rho_old, *rho_tmp_2, *rho_tmp_3, *rho_curr, *rhs_rho;
+  double *u_old, *u_tmp_2, *u_tmp_3, *u_curr, *u_fixed, *rhs_u, *tmp_1;
+  double *pres_old, *pres_tmp_2, *pres_tmp_3, *pres_fixed, *pres_fixed_old, *rhs_pres;
+  double *alpha;
+  double *pool = nullptr;
+};
+
+int solver_alloc(atm_ctx &c, Solver &s);
+void solver_free(Solver &s);
+int solver_step(atm_ctx &c, Solver &s);
+int solver_diagnostics(atm_ctx &c, Solver &s, double *out);
+
+}  // namespace atm

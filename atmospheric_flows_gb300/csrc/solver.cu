@@ -1,0 +1,198 @@
+// IMEX time loop on the device: EulerSolver::run and its stage solvers
+// (Atmospheric_Flow.cc:430-871, 1100-1257).
+//
+// Differences from the reference, by design:
+//   * the mass-type systems (rho mass, A, D) are block diagonal in this DG
+//     discretisation and are solved exactly with the per-cell inverse instead
+//     of CG + geometric multigrid to a tolerance (Atmospheric_Flow.cc:452-536,
+//     701-780, 801-870).  The answer is the reference's answer without the
+//     solver error.
+//   * inside the Schur apply A^{-1} is the exact per-cell inverse instead of
+//     CG + Jacobi to 1e-12 (euler_operator.h:2391-2397).
+//   * diagnostics and L2 error analysis are not part of the step (they are
+//     printouts in the reference, Atmospheric_Flow.cc:1121-1122,1225-1242);
+//     atm_solver_diagnostics computes them on demand.
+#include <cmath>
+
+#include "atm_device.cuh"
+
+namespace atm {
+
+int solver_alloc(atm_ctx &c, Solver &s) {
+  const long ns = c.n_scalar(), nv = c.n_vector();
+  const long total = 12 * ns + 7 * nv;
+  ATM_CUDA(cudaMalloc(&s.pool, total * sizeof(double)));
+  ATM_CUDA(cudaMemset(s.pool, 0, total * sizeof(double)));
+  double *p = s.pool;
+  auto take = [&](long n) { double *r = p; p += n; return r; };
+  s.rho_old = take(ns); s.rho_tmp_2 = take(ns); s.rho_tmp_3 = take(ns);
+  s.rho_curr = take(ns); s.rhs_rho = take(ns);
+  s.pres_old = take(ns); s.pres_tmp_2 = take(ns); s.pres_tmp_3 = take(ns);
+  s.pres_fixed = take(ns); s.pres_fixed_old = take(ns); s.rhs_pres = take(ns);
+  s.alpha = take(ns);
+  s.u_old = take(nv); s.u_tmp_2 = take(nv); s.u_tmp_3 = take(nv); s.u_curr = take(nv);
+  s.u_fixed = take(nv); s.rhs_u = take(nv); s.tmp_1 = take(nv);
+  return ATM_OK;
+}
+
+void solver_free(Solver &s) {
+  cudaFree(s.pool);
+  s.pool = nullptr;
+}
+
+namespace {
+
+#define TRY(x)              \
+  do {                      \
+    int _rc = (x);          \
+    if (_rc) return _rc;    \
+  } while (0)
+
+int set_rho_fixed(atm_ctx &c, const double *rho) {
+  TRY(vec_copy(c.stream, c.rho_fix, rho, c.n_scalar()));
+  return rebuild_ainv(c);
+}
+
+// Atmospheric_Flow.cc:430-537
+int update_density(atm_ctx &c, Solver &s) {
+  const StageCoef co = stage_coef_rho(c, c.hstage);
+  if (c.hstage == 1) {
+    const double *src[] = {s.rho_old, s.u_old};
+    TRY(launch_rhs_rho(c, 1, s.rhs_rho, src, co));
+    return launch_block_apply(c, s.rho_tmp_2, s.rhs_rho, c.mesh.minv, 1, 1.0);
+  } else if (c.hstage == 2) {
+    const double *src[] = {s.rho_old, s.u_old, s.rho_tmp_2, s.u_tmp_2};
+    TRY(launch_rhs_rho(c, 2, s.rhs_rho, src, co));
+    return launch_block_apply(c, s.rho_tmp_3, s.rhs_rho, c.mesh.minv, 1, 1.0);
+  }
+  const double *src[] = {s.rho_old, s.u_old, s.rho_tmp_2, s.u_tmp_2, s.rho_tmp_3, s.u_tmp_3};
+  TRY(launch_rhs_rho(c, 3, s.rhs_rho, src, co));
+  return launch_block_apply(c, s.rho_curr, s.rhs_rho, c.mesh.minv, 1, 1.0);
+}
+
+// Atmospheric_Flow.cc:544-673
+int pressure_fixed_point(atm_ctx &c, Solver &s) {
+  const long ns = c.n_scalar();
+  TRY(vec_copy(c.stream, c.pres_fix, s.pres_fixed_old, ns));  // set_pres_fixed
+  const StageCoef co = stage_coef_flux(c, c.hstage);
+  if (c.hstage == 1) {
+    const double *sp[] = {s.rho_old, s.u_old, s.pres_old, s.rho_tmp_2, s.u_fixed};
+    TRY(launch_rhs_pres(c, 1, s.rhs_pres, sp, co));
+    const double *su[] = {s.rho_old, s.u_old, s.pres_old, s.rho_tmp_2};
+    TRY(launch_rhs_vel(c, 1, s.rhs_u, su, co));
+  } else {
+    const double *sp[] = {s.rho_old, s.u_old, s.pres_old, s.rho_tmp_2, s.u_tmp_2,
+                          s.pres_tmp_2, s.rho_tmp_3, s.u_fixed};
+    TRY(launch_rhs_pres(c, 2, s.rhs_pres, sp, co));
+    const double *su[] = {s.rho_old, s.u_old, s.pres_old, s.rho_tmp_2, s.u_tmp_2,
+                          s.pres_tmp_2, s.rho_tmp_3};
+    TRY(launch_rhs_vel(c, 2, s.rhs_u, su, co));
+  }
+  // tmp_1 = A^{-1} rhs_u ; rhs_pres -= C tmp_1
+  TRY(launch_block_apply(c, s.tmp_1, s.rhs_u, c.ainv, 2, 1.0));
+  const double cc = implicit_coeff(c);
+  TRY(launch_CD(c, s.rhs_pres, s.tmp_1, nullptr, c.pres_fix, cc * c.dt, 3));
+  TRY(vec_dot(c.stream, s.rhs_pres, s.rhs_pres, ns, c.red, c.red_out));
+  TRY(read_scalars(c, 1));
+  const double tol = s.eps * std::sqrt(c.h_red[0]);
+  TRY(vec_copy(c.stream, s.pres_fixed, s.pres_fixed_old, ns));
+  int its = 0;
+  double res = 0.0;
+  int rc = gmres_schur(c, s.pres_fixed, s.rhs_pres, tol, s.max_its, &its, &res);
+  s.krylov_total += its;
+  if (rc == ATM_NOT_CONVERGED) { ++s.failures; rc = ATM_OK; }
+  return rc;
+}
+
+// Atmospheric_Flow.cc:680-781
+int update_velocity(atm_ctx &c, Solver &s) {
+  if (c.hstage == 1 || c.hstage == 2) {
+    const double co = implicit_coeff(c);
+    TRY(launch_B(c, s.rhs_u, s.pres_fixed, co * c.dt / (c.Ma * c.Ma), 1));
+    return launch_block_apply(c, s.u_fixed, s.rhs_u, c.ainv, 2, 1.0);
+  }
+  const StageCoef co = stage_coef_flux(c, 3);
+  const double *su[] = {s.rho_old, s.u_old, s.pres_old, s.rho_tmp_2, s.u_tmp_2,
+                        s.pres_tmp_2, s.rho_tmp_3, s.u_tmp_3, s.pres_tmp_3};
+  TRY(launch_rhs_vel(c, 3, s.rhs_u, su, co));
+  return launch_block_apply(c, s.u_curr, s.rhs_u, c.ainv, 2, 1.0);
+}
+
+// Atmospheric_Flow.cc:788-871
+int update_pressure(atm_ctx &c, Solver &s) {
+  const StageCoef co = stage_coef_flux(c, 3);
+  const double *sp[] = {s.rho_old, s.u_old, s.pres_old, s.rho_tmp_2, s.u_tmp_2,
+                        s.pres_tmp_2, s.rho_tmp_3, s.u_tmp_3, s.pres_tmp_3,
+                        s.rho_curr, s.u_curr};
+  TRY(launch_rhs_pres(c, 3, s.rhs_pres, sp, co));
+  return launch_block_apply(c, s.pres_old, s.rhs_pres, c.mesh.minv, 1, GAS_GAMMA - 1.0);
+}
+
+// Picard loop, Atmospheric_Flow.cc:1135-1153 / 1176-1194
+int picard(atm_ctx &c, Solver &s, int which) {
+  const long ns = c.n_scalar();
+  int iters = 0;
+  for (int iter = 0; iter < 100; ++iter) {
+    TRY(pressure_fixed_point(c, s));
+    TRY(update_velocity(c, s));
+    ++iters;
+    TRY(vec_maxdiff(c.stream, s.pres_fixed, s.pres_fixed_old, ns, c.red, c.red_out));
+    TRY(read_scalars(c, 2));
+    const double den = c.h_red[1];
+    const double error = c.h_red[0] / (den + 1e-10);
+    if (!std::isfinite(error)) { set_error("Picard: non-finite pressure"); return ATM_NONFINITE; }
+    if (error < 1e-10) break;
+    TRY(vec_copy(c.stream, s.pres_fixed_old, s.pres_fixed, ns));
+  }
+  s.last_picard[which] = iters;
+  s.picard_total += iters;
+  return ATM_OK;
+}
+
+}  // namespace
+
+// one pass of the while loop of Atmospheric_Flow.cc:1110-1250
+int solver_step(atm_ctx &c, Solver &s) {
+  const long ns = c.n_scalar(), nv = c.n_vector();
+  s.time += c.dt;
+  ++s.steps;
+  // stage 1
+  c.hstage = 1;
+  TRY(update_density(c, s));
+  TRY(set_rho_fixed(c, s.rho_tmp_2));
+  TRY(vec_copy(c.stream, s.pres_fixed_old, s.pres_old, ns));
+  TRY(vec_copy(c.stream, s.u_fixed, s.u_old, nv));
+  TRY(picard(c, s, 0));
+  TRY(vec_copy(c.stream, s.pres_tmp_2, s.pres_fixed, ns));
+  TRY(vec_copy(c.stream, s.u_tmp_2, s.u_fixed, nv));
+  // stage 2
+  c.hstage = 2;
+  TRY(update_density(c, s));
+  TRY(set_rho_fixed(c, s.rho_tmp_3));
+  TRY(vec_copy(c.stream, s.pres_fixed_old, s.pres_tmp_2, ns));
+  TRY(vec_copy(c.stream, s.u_fixed, s.u_tmp_2, nv));
+  TRY(picard(c, s, 1));
+  TRY(vec_copy(c.stream, s.pres_tmp_3, s.pres_fixed, ns));
+  TRY(vec_copy(c.stream, s.u_tmp_3, s.u_fixed, nv));
+  // stage 3 (final combination)
+  c.hstage = 3;
+  TRY(update_density(c, s));
+  TRY(set_rho_fixed(c, s.rho_curr));
+  TRY(update_velocity(c, s));
+  TRY(update_pressure(c, s));
+  TRY(vec_copy(c.stream, s.rho_old, s.rho_curr, ns));
+  TRY(vec_copy(c.stream, s.u_old, s.u_curr, nv));
+  if (s.sponge)
+    TRY(vec_sponge(c.stream, s.u_old, s.alpha, c.dt, s.ubg0, s.ubg1, c.nc, c.nn2));
+  return ATM_OK;
+}
+
+int solver_diagnostics(atm_ctx &c, Solver &s, double *out) {
+  TRY(vec_diagnostics(c.stream, s.rho_old, s.u_old, s.pres_old, c.nc, c.nn2, c.red,
+                      c.red_out));
+  TRY(read_scalars(c, 4));
+  for (int i = 0; i < 4; ++i) out[i] = c.h_red[i];
+  return ATM_OK;
+}
+
+}  // namespace atm

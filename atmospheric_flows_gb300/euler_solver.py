@@ -1,0 +1,68 @@
+"""Python mirror of the reference's ``EulerSolver`` (Atmospheric_Flow.cc:57-1257).
+
+The time loop itself runs in the library (C++ host code driving sm_103a
+kernels); this class owns the device context, uploads the case and moves
+state between host arrays and the device.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .euler_operator import EULEROperator, MatrixFreeStorage
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def _d(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+class EulerSolver:
+    """IMEX-DG solver for one member (one device context)."""
+
+    PRECISION_FP64 = 0
+    PRECISION_MIXED = 1
+
+    def __init__(self, case, eps=1e-8, max_its=30000, precision=0, dt=None):
+        self.case = case
+        self.op = EULEROperator(MatrixFreeStorage.from_case(case))
+        self.dt = case.dt if dt is None else float(dt)
+        _lib.call("atm_solver_init", self.op.handle, self.dt, case.Ma, case.Fr, float(eps),
+                  int(max_its), int(precision))
+        self.n_scalar = self.op.n_scalar
+        self.set_state(case.rho, case.u, case.p)
+        alpha = np.ascontiguousarray(case.sponge_alpha, dtype=np.float64)
+        if np.any(alpha > 0):
+            _lib.call("atm_solver_set_sponge", self.op.handle, _d(alpha), case.params.u0, 0.0)
+
+    def set_state(self, rho, u, p):
+        r, uu, pp = (np.ascontiguousarray(a, dtype=np.float64) for a in (rho, u, p))
+        _lib.call("atm_solver_set_state", self.op.handle, _d(r), _d(uu), _d(pp))
+
+    def get_state(self):
+        ns = self.n_scalar
+        r, u, p = np.empty(ns), np.empty(2 * ns), np.empty(ns)
+        _lib.call("atm_solver_get_state", self.op.handle, _d(r), _d(u), _d(p))
+        return r, u, p
+
+    def run(self, n_steps):
+        _lib.call("atm_solver_run", self.op.handle, int(n_steps))
+
+    def stats(self):
+        s = np.zeros(8)
+        _lib.call("atm_solver_stats", self.op.handle, _d(s))
+        keys = ("steps", "picard_total", "krylov_total", "picard_stage1", "picard_stage2",
+                "solve_fail", "time", "dt")
+        return dict(zip(keys, s.tolist()))
+
+    def diagnostics(self):
+        out = np.zeros(4)
+        _lib.call("atm_solver_diagnostics", self.op.handle, _d(out))
+        return dict(zip(("min_rho", "max_rho", "max_celerity", "max_velocity"), out.tolist()))
+
+    def close(self):
+        self.op.close()

@@ -1,0 +1,176 @@
+/*
+ * atm_gb300.h -- C ABI of the GB300 IMEX-DG dynamical-core hot path.
+ *
+ * The entry points replace the matrix-free operator and the stage solvers of
+ * GiuseppeOrlando878776/Atmospheric_Flows (a deal.II code).  Each block below
+ * names the reference interface it stands in for (file:line in that project).
+ * All arithmetic is FP64 unless an entry point says otherwise.
+ *
+ * Conventions
+ *   - Every call returns an int status (ATM_OK = 0); no C++ exception crosses
+ *     the ABI.  atm_last_error() gives a message for the last failure.
+ *   - dim = 2, degree k in 1..5, quadrature QGauss(2k+1) for every integral.
+ *   - Field vectors are cell-contiguous: scalar fields [cell][node], velocity
+ *     [cell][component][node], node = iz*(k+1)+ix on Gauss-Lobatto points
+ *     (the layout of FE_DGQ / FESystem(FE_DGQ,dim) blocks).
+ *   - Operator entry points (atm_vmult*, atm_set_*_fixed, atm_solve*) take
+ *     DEVICE pointers and run asynchronously on the context's stream; the
+ *     destination is overwritten (deal.II loop(..., zero_dst=true)).
+ *   - The solver-level entry points (atm_solver_*) take HOST pointers.
+ *   - A handle is not thread-safe; several handles may be used from one
+ *     host thread.
+ */
+#ifndef ATM_GB300_H
+#define ATM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum atm_status {
+  ATM_OK = 0,
+  ATM_BAD_ARG = 1,
+  ATM_NOT_CONVERGED = 2,
+  ATM_NONFINITE = 3,
+  ATM_OOM = 4,
+  ATM_TIMEOUT = 5,
+  ATM_CUDA_ERROR = 6,
+  ATM_NOT_READY = 7
+};
+
+typedef struct atm_ctx *atm_handle;
+
+/* Message of the last failing call on this thread (never NULL). */
+const char *atm_last_error(void);
+/* Library version string. */
+const char *atm_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Context = EULEROperator + its MatrixFree storage.
+ * Replaces: MatrixFree::reinit / EULEROperator::initialize
+ *   (Atmospheric_Flow.cc:325-348,435), the mesh/dof set-up
+ *   (Atmospheric_Flow.cc:279-409) re-uploaded as plain tables.
+ *   mapping_nodes : [n_cells][(m+1)^2][2] host, Gauss-Lobatto points of a
+ *                   degree-m tensor Lagrange mapping (MappingQ(m)), x fastest
+ *   inner_faces   : [n_inner][5] host: cell+, face+, cell-, face-, orientation
+ *                   (local faces 0:x=0 1:x=1 2:z=0 3:z=1; orientation must be 0)
+ *   bdry_faces    : [n_bdry][3] host: cell, face, boundary id (all walls)
+ * ------------------------------------------------------------------------- */
+int atm_ctx_create(int dim, int degree, int n_cells, int mapping_degree,
+                   const double *mapping_nodes, int n_inner, const int *inner_faces,
+                   int n_bdry, const int *bdry_faces, atm_handle *out);
+int atm_ctx_destroy(atm_handle h);
+/* Re-upload geometry and connectivity after mesh adaptation (same sizes). */
+int atm_upload_mesh(atm_handle h, int mapping_degree, const double *mapping_nodes,
+                    int n_inner, const int *inner_faces, int n_bdry,
+                    const int *bdry_faces);
+/* cudaStream_t as void*; NULL = the legacy default stream. */
+int atm_set_stream(atm_handle h, void *stream);
+int atm_synchronize(atm_handle h);
+/* Sizes: scalar field length n_cells*(k+1)^2; velocity twice that. */
+long atm_n_scalar(atm_handle h);
+
+/* Instrumentation (replaces deal.II TimerOutput, Atmospheric_Flow.cc:176-178,
+ * 249).  atm_kernel_launches counts every kernel launch of the library in
+ * this process.  With timing enabled, each operator launch is bracketed by
+ * CUDA events on the context's stream; atm_timing_read synchronises and
+ * returns, per family 0..8 = rhs_rho, rhs_vel, rhs_pres, B, C/D, mass,
+ * diagonal, block inverse, block apply: total ms, launches, algorithmic HBM
+ * bytes (fields read + written, 8 B per node value) and FP64 flops of the
+ * sum-factorisation contractions; then resets them.  Any output may be NULL. */
+long atm_kernel_launches(void);
+int atm_timing_enable(atm_handle h, int on);
+int atm_timing_read(atm_handle h, double *ms, long *launches, double *bytes, double *flops,
+                    int n);
+
+/* ---------------------------------------------------------------------------
+ * Setters.  Replace EULEROperator::set_dt / set_Mach / set_Froude /
+ * set_HYPERBOLIC_stage / set_NS_stage (euler_operator.h:34-43,245-303).
+ * ------------------------------------------------------------------------- */
+int atm_set_dt(atm_handle h, double dt);
+int atm_set_mach(atm_handle h, double mach);
+int atm_set_froude(atm_handle h, double froude);
+int atm_set_hyperbolic_stage(atm_handle h, int stage); /* 1..3 */
+int atm_set_ns_stage(atm_handle h, int stage);         /* 1..6 */
+
+/* Frozen fields (device pointers, copied).  Replace set_rho_for_fixed /
+ * set_pres_fixed / set_u_fixed (euler_operator.h:45-52,306-339).
+ * set_rho_for_fixed also rebuilds the exact cell-wise inverse of
+ * A = (rho_fix-weighted velocity mass) used by the Schur apply and solves. */
+int atm_set_rho_for_fixed(atm_handle h, const double *rho);
+int atm_set_pres_fixed(atm_handle h, const double *pres);
+int atm_set_u_fixed(atm_handle h, const double *u);
+
+/* ---------------------------------------------------------------------------
+ * Explicit stage right-hand sides (device pointers).  Replace
+ *   vmult_rhs_rho_update      euler_operator.h:54-55,697-712
+ *   vmult_rhs_velocity_fixed  euler_operator.h:60-61,2310-2325
+ *   vmult_rhs_pressure        euler_operator.h:57-58,1366-1381
+ * src is the positional source list of the reference call sites
+ * (Atmospheric_Flow.cc:439-449,555-568,696-698,796-799); nsrc must be
+ *   rho: 2 / 4 / 6, velocity: 4 / 7 / 9, pressure: 5 / 8 / 11
+ * for IMEX stage 1 / 2 / 3.
+ * ------------------------------------------------------------------------- */
+int atm_vmult_rhs_rho_update(atm_handle h, double *dst, const double *const *src, int nsrc);
+int atm_vmult_rhs_velocity_fixed(atm_handle h, double *dst, const double *const *src,
+                                 int nsrc);
+int atm_vmult_rhs_pressure(atm_handle h, double *dst, const double *const *src, int nsrc);
+
+/* B: pressure -> velocity space.  Replaces vmult_pressure
+ * (euler_operator.h:63,1512-1617,2422-2435). */
+int atm_vmult_pressure(atm_handle h, double *dst, const double *src);
+/* C: velocity -> pressure space, with pres_fixed.  Replaces vmult_enthalpy
+ * (euler_operator.h:65,1413-1507,2440-2453). */
+int atm_vmult_enthalpy(atm_handle h, double *dst, const double *src);
+/* Base::vmult -> apply_add for the current NS stage
+ * (euler_operator.h:93,2366-2417): NS 1/4 rho mass, NS 2 Schur
+ * S p = D p - C A^{-1} B p (A^{-1} exact per cell), NS 3/5 A, NS 6 D. */
+int atm_vmult(atm_handle h, double *dst, const double *src);
+/* compute_diagonal + get_matrix_diagonal_inverse (euler_operator.h:67,
+ * 2458-2626): writes the inverse diagonal for the current NS stage
+ * (NS 2 uses the diagonal of D only, as the reference does). */
+int atm_diagonal_inverse(atm_handle h, double *dst);
+
+/* Solve op x = b for the current NS stage.  Replaces the stage solvers'
+ * SolverCG+PreconditionMG (mass systems, solved here exactly with the
+ * cell-wise inverse) and SolverGMRES+PreconditionJacobi (NS 2)
+ * (Atmospheric_Flow.cc:452-536,642,656-672,701-780,801-870).  x holds the
+ * initial guess.  tol is absolute on the (Jacobi-preconditioned) residual;
+ * iters/res may be NULL.  Returns ATM_NOT_CONVERGED on maxit. */
+int atm_solve(atm_handle h, double *x, const double *b, double tol, int maxit,
+              int *iters, double *res);
+
+/* ---------------------------------------------------------------------------
+ * Time loop.  Replaces EulerSolver (Atmospheric_Flow.cc:57-272,1100-1257):
+ * the 3-stage IMEX step with the Picard loop (<= 100 iterations, 1e-10
+ * relative L-infinity stop), stage combination and an optional Rayleigh
+ * sponge on u (applied after stage 3).  The solver state lives in the
+ * context (one solver per context); set/get use HOST pointers unless the
+ * name ends in _device.
+ *   precision: 0 = FP64 GMRES + Jacobi (the reference solver),
+ *              1 = FP64 flexible GMRES with an FP32 multigrid preconditioner.
+ * ------------------------------------------------------------------------- */
+int atm_solver_init(atm_handle h, double dt, double mach, double froude, double eps,
+                    int max_its, int precision);
+int atm_solver_set_state(atm_handle h, const double *rho, const double *u,
+                         const double *p);
+int atm_solver_get_state(atm_handle h, double *rho, double *u, double *p);
+/* device-pointer variants (length n_scalar / 2*n_scalar / n_scalar) */
+int atm_solver_set_state_device(atm_handle h, const double *rho, const double *u,
+                                const double *p);
+int atm_solver_get_state_device(atm_handle h, double *rho, double *u, double *p);
+int atm_solver_set_sponge(atm_handle h, const double *alpha_nodes, double ubg_x,
+                          double ubg_z);
+int atm_solver_run(atm_handle h, int n_steps);
+/* stats[0..7] as doubles: steps, Picard iterations (total), Krylov
+ * iterations (total), last Picard count stage 1, stage 2, Krylov solves that
+ * hit max_its, simulated time, current dt. */
+int atm_solver_stats(atm_handle h, double *stats);
+/* Diagnostics of Atmospheric_Flow.cc:991-1087 at the Gauss-Lobatto nodes:
+ * out[0..3] = min rho, max |rho|, max sqrt(gamma p/rho), max |u|. */
+int atm_solver_diagnostics(atm_handle h, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ATM_GB300_H */

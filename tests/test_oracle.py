@@ -1,0 +1,196 @@
+"""Pins for the CPU oracle (no GPU).
+
+The reference's own FP64 deal.II run cannot be executed here (deal.II, MPI
+and p4est are absent) and the reference ships no golden vectors, so the
+oracle is pinned by properties that the restated discretisation must satisfy
+exactly: quadrature/basis identities, discrete conservation, the
+integration-by-parts identity between B and C, operator identities at rest,
+and the golden fixture it produced when it was first pinned.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from atmospheric_flows_gb300.hill import HillParams, build_case, gll_points
+from oracle.oracle import OracleOperator, OracleSolver
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def rel(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def perturbed(case, seed=1, amp=0.01):
+    rng = np.random.default_rng(seed)
+    rho = case.rho * (1 + amp * rng.standard_normal(case.rho.shape))
+    u = case.u + 2.0 * rng.standard_normal(case.u.shape)
+    p = case.p * (1 + amp * rng.standard_normal(case.p.shape))
+    return rho, u, p
+
+
+@pytest.fixture(scope="module")
+def flat_case():
+    return build_case(HillParams(nx=6, nz=3, degree=3, h0=0.0, cfl=1.0))
+
+
+@pytest.fixture(scope="module")
+def hill_case():
+    return build_case(HillParams(nx=6, nz=4, degree=4, cfl=2.0))
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5])
+def test_basis_identities(k):
+    case = build_case(HillParams(nx=2, nz=1, degree=k))
+    op = OracleOperator(case)
+    S, D, W = op.basis()
+    assert abs(W.sum() - 1.0) < 1e-14
+    assert np.allclose(S.sum(axis=1), 1.0, atol=1e-13)
+    assert np.allclose(D.sum(axis=1), 0.0, atol=1e-11)
+    # Gauss(2k+1) integrates x^p exactly up to p = 4k+1
+    nq = 2 * k + 1
+    _, _, _ = S, D, W
+    x = np.array([(S[q] * gll_points(k)).sum() for q in range(nq)])  # nodes reproduce x
+    for pw in range(0, 4 * k + 2):
+        assert abs((W * x ** pw).sum() - 1.0 / (pw + 1)) < 1e-13
+
+
+def test_gll_known_values():
+    g = gll_points(4) * 2 - 1
+    assert np.allclose(g, [-1, -np.sqrt(3 / 7), 0, np.sqrt(3 / 7), 1], atol=1e-15)
+
+
+def test_mass_area_flat(flat_case):
+    op = OracleOperator(flat_case)
+    op.set_stage(1, 1)
+    m1 = op.vmult(np.ones(op.n_scalar))
+    area = (flat_case.params.x1 - flat_case.params.x0) * flat_case.params.height
+    assert abs(m1.sum() - area) / area < 1e-13
+
+
+@pytest.mark.parametrize("stage", [1, 2, 3])
+def test_rho_rhs_at_rest_is_mass(hill_case, stage):
+    op = OracleOperator(hill_case)
+    op.set_stage(stage, 1)
+    rho, u, p = perturbed(hill_case)
+    zero = np.zeros_like(u)
+    src = [rho, zero] * stage
+    r = op.vmult_rhs_rho_update(src)
+    assert rel(r, op.vmult(rho)) < 1e-14
+
+
+@pytest.mark.parametrize("stage", [1, 2, 3])
+def test_rho_rhs_conserves_mass(hill_case, stage):
+    op = OracleOperator(hill_case)
+    op.set_stage(stage, 1)
+    rho, u, p = perturbed(hill_case)
+    src = []
+    for j in range(stage):
+        src += [rho * (1 + 0.1 * j), u * (1 - 0.2 * j)]
+    r = op.vmult_rhs_rho_update(src)
+    m = op.vmult(rho)
+    assert abs(r.sum() - m.sum()) / abs(m.sum()) < 1e-13
+
+
+def test_energy_rhs_at_rest_is_D(hill_case):
+    op = OracleOperator(hill_case)
+    rho, _, p = perturbed(hill_case)
+    z = np.zeros(2 * op.n_scalar)
+    op.set_stage(1, 6)
+    r = op.vmult_rhs_pressure([rho, z, p, rho, z])
+    assert rel(r, op.vmult(p)) < 1e-13
+
+
+def test_momentum_constant_pressure_balances(flat_case):
+    # no gravity (huge Fr), u = 0, constant p: the pressure terms integrate to 0
+    op = OracleOperator(flat_case)
+    op.set_params(flat_case.dt, flat_case.Ma, 1e30)
+    n = op.n_scalar
+    z = np.zeros(2 * n)
+    p = np.full(n, 0.8)
+    op.set_stage(1, 3)
+    r = op.vmult_rhs_velocity_fixed([np.ones(n), z, p, np.ones(n)])
+    scale = flat_case.dt / flat_case.Ma ** 2 * 0.8 * 1e4
+    assert np.max(np.abs(r)) / scale < 1e-12
+
+
+def test_B_C_integration_by_parts(flat_case):
+    # <B q, w> Ma^2/(c dt) = -<C w, q>/(c dt hg pfix) for constant pfix on an
+    # affine mesh (exact quadrature, central flux; the upwind term vanishes)
+    op = OracleOperator(flat_case)
+    rng = np.random.default_rng(3)
+    n = op.n_scalar
+    pf = 0.9
+    op.set_pres_fixed(np.full(n, pf))
+    for hs in (1, 2):
+        op.set_stage(hs, 2)
+        q = rng.standard_normal(n)
+        w = rng.standard_normal(2 * n)
+        Bq = op.vmult_pressure(q)
+        Cw = op.vmult_enthalpy(w)
+        c = op.case.Ma  # noqa: F841
+        g = 1.4
+        lhs = np.dot(Bq, w) * flat_case.Ma ** 2
+        rhs = -np.dot(Cw, q) / (g / (g - 1) * pf)
+        assert abs(lhs - rhs) / abs(lhs) < 1e-11
+
+
+def test_diagonal_matches_probing():
+    case = build_case(HillParams(nx=2, nz=1, degree=2))
+    op = OracleOperator(case)
+    rho, _, _ = perturbed(case)
+    op.set_rho_for_fixed(rho)
+    for ns in (1, 3, 6):
+        op.set_stage(1, ns)
+        n = op.n_scalar * (2 if ns == 3 else 1)
+        d = np.array([op.vmult(np.eye(1, n, i).ravel())[i] for i in range(n)])
+        assert rel(1.0 / op.diagonal_inverse(), d) < 1e-13
+
+
+def test_schur_definition(hill_case):
+    op = OracleOperator(hill_case)
+    rho, u, p = perturbed(hill_case)
+    op.set_rho_for_fixed(rho)
+    op.set_pres_fixed(p)
+    op.set_inner_tol(1e-15)
+    op.set_stage(2, 2)
+    x = np.random.default_rng(5).standard_normal(op.n_scalar)
+    s = op.vmult(x)
+    op.set_stage(2, 6)
+    dx = op.vmult(x)
+    op.set_stage(2, 3)
+    t1 = op.vmult_pressure(x)
+    t2, rc, _ = op.solve(t1, tol=1e-15 * np.linalg.norm(t1))
+    assert rc == 0
+    ref = dx - op.vmult_enthalpy(t2)
+    assert rel(s, ref) < 1e-10
+
+
+def test_time_loop_conserves_mass(hill_case):
+    s = OracleSolver(hill_case, eps=1e-12, inner_tol=1e-14)
+    op = OracleOperator(hill_case)
+    op.set_stage(1, 1)
+    m0 = op.vmult(hill_case.rho).sum()
+    s.run(2)
+    rho, u, p = s.get_state()
+    m1 = op.vmult(rho).sum()
+    assert abs(m1 - m0) / m0 < 1e-11
+    st = s.stats()
+    assert st["solve_fail"] == 0 and st["picard_stage1"] >= 1
+
+
+def test_golden_fixture_regression():
+    """The oracle reproduces the fixture written by tests/golden/make_golden.py."""
+    path = os.path.join(GOLDEN, "oracle_hill_k3.npz")
+    if not os.path.exists(path):
+        pytest.skip("golden fixture not generated")
+    g = np.load(path)
+    case = build_case(HillParams(nx=int(g["nx"]), nz=int(g["nz"]), degree=int(g["k"]),
+                                 cfl=float(g["cfl"])))
+    s = OracleSolver(case, eps=float(g["eps"]), inner_tol=float(g["inner_tol"]))
+    s.run(int(g["steps"]))
+    rho, u, p = s.get_state()
+    for name, v in (("rho", rho), ("u", u), ("p", p)):
+        ref = g[name]
+        assert np.linalg.norm(v - ref) / np.linalg.norm(ref) < 1e-11, name
