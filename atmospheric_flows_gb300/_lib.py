@@ -28,6 +28,7 @@ SIGNATURES = {
     "atm_synchronize": (_i, [_h]),
     "atm_n_scalar": (ctypes.c_long, [_h]),
     "atm_kernel_launches": (ctypes.c_long, []),
+    "atm_probe_fma_peak": (_i, [_dp, _dp]),
     "atm_timing_enable": (_i, [_h, _i]),
     "atm_timing_read": (_i, [_h, _dp, ctypes.POINTER(ctypes.c_long), _dp, _dp, _i]),
     "atm_set_dt": (_i, [_h, _d]),

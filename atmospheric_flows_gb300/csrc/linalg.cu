@@ -91,26 +91,41 @@ __global__ void k_finalize(const double *__restrict__ red, double *__restrict__ 
   if (threadIdx.x == 0) out[blockIdx.x] = acc;
 }
 
-__global__ void k_multidot_partial(const double *__restrict__ V, long ldv, int m,
+// M vectors per pass: fixed-size accumulators stay in registers
+template <int M>
+__global__ void k_multidot_partial(const double *__restrict__ V, long ldv,
                                    const double *__restrict__ w, long n,
                                    double *__restrict__ red) {
   __shared__ double sh[RT / 32];
-  double acc[MAXM];
+  double acc[M];
 #pragma unroll
-  for (int l = 0; l < MAXM; ++l) acc[l] = 0.0;
+  for (int l = 0; l < M; ++l) acc[l] = 0.0;
   for (long i = (long)blockIdx.x * RT + threadIdx.x; i < n; i += (long)RED_BLOCKS * RT) {
     const double wi = w[i];
 #pragma unroll
-    for (int l = 0; l < MAXM; ++l)
-      if (l < m) acc[l] = fma(V[l * ldv + i], wi, acc[l]);
+    for (int l = 0; l < M; ++l) acc[l] = fma(V[l * ldv + i], wi, acc[l]);
   }
 #pragma unroll
-  for (int l = 0; l < MAXM; ++l) {
-    if (l < m) {
-      const double s = block_reduce<0>(acc[l], sh);
-      if (threadIdx.x == 0) red[(long)l * RED_BLOCKS + blockIdx.x] = s;
-    }
+  for (int l = 0; l < M; ++l) {
+    const double s = block_reduce<0>(acc[l], sh);
+    if (threadIdx.x == 0) red[(long)l * RED_BLOCKS + blockIdx.x] = s;
   }
+}
+
+// up to 8 vectors per launch; larger m is split into chunks of 8
+void multidot_chunk(cudaStream_t st, const double *V, long ldv, int m, const double *w,
+                    long n, double *red) {
+  switch (m) {
+    case 1: k_multidot_partial<1><<<RED_BLOCKS, RT, 0, st>>>(V, ldv, w, n, red); break;
+    case 2: k_multidot_partial<2><<<RED_BLOCKS, RT, 0, st>>>(V, ldv, w, n, red); break;
+    case 3: k_multidot_partial<3><<<RED_BLOCKS, RT, 0, st>>>(V, ldv, w, n, red); break;
+    case 4: k_multidot_partial<4><<<RED_BLOCKS, RT, 0, st>>>(V, ldv, w, n, red); break;
+    case 5: k_multidot_partial<5><<<RED_BLOCKS, RT, 0, st>>>(V, ldv, w, n, red); break;
+    case 6: k_multidot_partial<6><<<RED_BLOCKS, RT, 0, st>>>(V, ldv, w, n, red); break;
+    case 7: k_multidot_partial<7><<<RED_BLOCKS, RT, 0, st>>>(V, ldv, w, n, red); break;
+    default: k_multidot_partial<8><<<RED_BLOCKS, RT, 0, st>>>(V, ldv, w, n, red); break;
+  }
+  g_kernel_launches.fetch_add(1);
 }
 
 __global__ void k_multiaxpy(double *__restrict__ w, const double *__restrict__ V, long ldv,
@@ -222,7 +237,10 @@ int vec_dot(cudaStream_t st, const double *x, const double *y, long n, double *r
 int vec_multidot(cudaStream_t st, const double *V, long ldv, int m, const double *w, long n,
                  double *red, double *out) {
   if (m < 1 || m > MAXM) return ATM_BAD_ARG;
-  k_multidot_partial<<<RED_BLOCKS, RT, 0, st>>>(V, ldv, m, w, n, red);
+  for (int l0 = 0; l0 < m; l0 += 8) {
+    const int mm = m - l0 < 8 ? m - l0 : 8;
+    multidot_chunk(st, V + (long)l0 * ldv, ldv, mm, w, n, red + (long)l0 * RED_BLOCKS);
+  }
   k_finalize<0><<<m, RT, 0, st>>>(red, out);
   ATM_CHECK_LAUNCH("vec_multidot");
   return ATM_OK;
@@ -258,3 +276,55 @@ int vec_sponge(cudaStream_t st, double *u, const double *alpha, double dt, doubl
 }
 
 }  // namespace atm
+
+// ------------------------------------------------------------------------
+// FMA throughput probe: 8 independent FMA chains per thread on a grid of
+// 8 blocks per SM; used to measure the FP64 / FP32 denominators of the
+// compute roofline on the machine the bench runs on.
+namespace atm {
+namespace {
+template <typename T>
+__global__ void k_fma_probe(T *out, int iters, T a, T b) {
+  T x0 = (T)threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  T x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+template <typename T>
+int probe(int iters, double *gflops) {
+  int dev = 0, nsm = 0;
+  ATM_CUDA(cudaGetDevice(&dev));
+  ATM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = nsm * 8, threads = 256;
+  T *out = nullptr;
+  ATM_CUDA(cudaMalloc(&out, sizeof(T) * blocks * threads));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_fma_probe<T><<<blocks, threads>>>(out, 16, (T)0.999, (T)0.001);
+  cudaEventRecord(e0);
+  k_fma_probe<T><<<blocks, threads>>>(out, iters, (T)0.999, (T)0.001);
+  cudaEventRecord(e1);
+  cudaError_t err = cudaEventSynchronize(e1);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  g_kernel_launches.fetch_add(2);
+  if (err != cudaSuccess) return cuda_fail(err, "fma probe");
+  *gflops = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e9;
+  return ATM_OK;
+}
+}  // namespace
+}  // namespace atm
+
+extern "C" int atm_probe_fma_peak(double *fp64_gflops, double *fp32_gflops) {
+  if (!fp64_gflops || !fp32_gflops) return ATM_BAD_ARG;
+  int rc = atm::probe<double>(4000, fp64_gflops);
+  if (rc) return rc;
+  return atm::probe<float>(100000, fp32_gflops);
+}

@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--eps", type=float, default=1e-8)
     ap.add_argument("--precision", default="fp64", choices=["fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fma-probe", action="store_true",
+                    help="print the measured FP64/FP32 FMA peaks and exit")
     return ap.parse_args()
 
 
@@ -308,8 +310,23 @@ def run_gb300(args):
     return 0
 
 
+def fma_probe():
+    import torch
+
+    from atmospheric_flows_gb300 import _lib
+
+    torch.cuda.set_device(0)
+    f64, f32 = ctypes.c_double(), ctypes.c_double()
+    _lib.call("atm_probe_fma_peak", ctypes.byref(f64), ctypes.byref(f32))
+    print(json.dumps({"fp64_fma_gflops": f64.value, "fp32_fma_gflops": f32.value,
+                      "ratio": f32.value / f64.value}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.fma_probe:
+        return fma_probe()
     if args.impl == "reference":
         return run_reference(args)
     return run_gb300(args)

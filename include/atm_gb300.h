@@ -79,6 +79,9 @@ long atm_n_scalar(atm_handle h);
  * bytes (fields read + written, 8 B per node value) and FP64 flops of the
  * sum-factorisation contractions; then resets them.  Any output may be NULL. */
 long atm_kernel_launches(void);
+/* FP64 and FP32 FMA throughput of the current device in GFLOP/s (independent
+ * FMA chains, 8 blocks per SM); the compute-roofline denominators. */
+int atm_probe_fma_peak(double *fp64_gflops, double *fp32_gflops);
 int atm_timing_enable(atm_handle h, int on);
 int atm_timing_read(atm_handle h, double *ms, long *launches, double *bytes, double *flops,
                     int n);
