@@ -45,6 +45,7 @@ SIGNATURES = {
     "atm_vmult_pressure": (_i, [_h, ctypes.c_void_p, ctypes.c_void_p]),
     "atm_vmult_enthalpy": (_i, [_h, ctypes.c_void_p, ctypes.c_void_p]),
     "atm_vmult": (_i, [_h, ctypes.c_void_p, ctypes.c_void_p]),
+    "atm_schur_vmult_static_scratch": (_i, [_h, ctypes.c_void_p, ctypes.c_void_p]),
     "atm_diagonal_inverse": (_i, [_h, ctypes.c_void_p]),
     "atm_solve": (_i, [_h, ctypes.c_void_p, ctypes.c_void_p, _d, _i, _ip, _dp]),
     "atm_solver_init": (_i, [_h, _d, _d, _d, _d, _i, _i]),

@@ -134,6 +134,18 @@ int atm_vmult(atm_handle h, double *dst, const double *src);
  * (NS 2 uses the diagonal of D only, as the reference does). */
 int atm_diagonal_inverse(atm_handle h, double *dst);
 
+/* Schur apply S p = D p - C A^{-1} B p (same result as atm_vmult in NS
+ * stage 2) that allocates nothing: the intermediate A^{-1} B p is kept in a
+ * static 8 MiB device array owned by the library.  For callers that must not
+ * have the library allocate device memory at call time (a host that owns all
+ * HBM through its own pool or budget; loops that cannot afford the device-wide
+ * synchronisation of cudaMalloc/cudaFree).  No counterpart in the reference.
+ * Limits: 2*n_scalar <= 1048576 doubles, else ATM_BAD_ARG; all calls on a
+ * device share the array, so calls that overlap on the GPU race; the first
+ * call on a device looks the array up and should come before any stream
+ * capture; kernel timing must be off.  Device pointers, context's stream. */
+int atm_schur_vmult_static_scratch(atm_handle h, double *dst, const double *src);
+
 /* Solve op x = b for the current NS stage.  Replaces the stage solvers'
  * SolverCG+PreconditionMG (mass systems, solved here exactly with the
  * cell-wise inverse) and SolverGMRES+PreconditionJacobi (NS 2)
