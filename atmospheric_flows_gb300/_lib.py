@@ -48,6 +48,11 @@ SIGNATURES = {
     "atm_schur_vmult_static_scratch": (_i, [_h, ctypes.c_void_p, ctypes.c_void_p]),
     "atm_diagonal_inverse": (_i, [_h, ctypes.c_void_p]),
     "atm_solve": (_i, [_h, ctypes.c_void_p, ctypes.c_void_p, _d, _i, _ip, _dp]),
+    "atm_mg_add_level": (_i, [_h, _i, _i, _dp, _i, _ip, _i, _ip, _ip]),
+    "atm_mg_set_smoother": (_i, [_h, _i, _d, _i, _i]),
+    "atm_mg_vcycle": (_i, [_h, _i, ctypes.c_void_p, ctypes.c_void_p]),
+    "atm_solve_fgmres": (_i, [_h, _i, ctypes.c_void_p, ctypes.c_void_p, _d, _i, _ip, _dp]),
+    "atm_set_true_residual_check": (_i, [_h, _i]),
     "atm_solver_init": (_i, [_h, _d, _d, _d, _d, _i, _i]),
     "atm_solver_set_state": (_i, [_h, _dp, _dp, _dp]),
     "atm_solver_get_state": (_i, [_h, _dp, _dp, _dp]),
@@ -60,7 +65,7 @@ SIGNATURES = {
 }
 
 KERNEL_FAMILIES = ("rhs_rho", "rhs_vel", "rhs_pres", "B", "CD", "mass", "diag",
-                   "block_inverse", "block_apply")
+                   "block_inverse", "block_apply", "mg_level_apply", "mg_vcycle")
 
 STATUS = {0: "OK", 1: "BAD_ARG", 2: "NOT_CONVERGED", 3: "NONFINITE", 4: "OOM", 5: "TIMEOUT",
           6: "CUDA_ERROR", 7: "NOT_READY"}

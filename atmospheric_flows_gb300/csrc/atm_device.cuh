@@ -31,15 +31,30 @@ struct Cfg {
 // [degree][0: values, 1: derivatives][q*(k+1)+i] at the 2k+1 Gauss points.
 // Each translation unit holds its own copy in its constant bank.
 static __constant__ double c_basis[KMAX + 1][2][NQ_MAX * NN_MAX];
+static __constant__ float c_basis_f[KMAX + 1][2][NQ_MAX * NN_MAX];
 
 static inline int upload_basis_here(const double *table) {
-  return cudaMemcpyToSymbol(c_basis, table, sizeof(c_basis)) == cudaSuccess ? 0 : 1;
+  float tf[(KMAX + 1) * 2 * NQ_MAX * NN_MAX];
+  for (int i = 0; i < (KMAX + 1) * 2 * NQ_MAX * NN_MAX; ++i) tf[i] = (float)table[i];
+  if (cudaMemcpyToSymbol(c_basis, table, sizeof(c_basis)) != cudaSuccess) return 1;
+  return cudaMemcpyToSymbol(c_basis_f, tf, sizeof(c_basis_f)) == cudaSuccess ? 0 : 1;
 }
 
-template <int K>
-__device__ __forceinline__ double bS(int q, int i) { return c_basis[K][0][q * (K + 1) + i]; }
-template <int K>
-__device__ __forceinline__ double bD(int q, int i) { return c_basis[K][1][q * (K + 1) + i]; }
+template <typename T>
+struct CBasis;
+template <>
+struct CBasis<double> {
+  static __device__ __forceinline__ double get(int k, int w, int idx) { return c_basis[k][w][idx]; }
+};
+template <>
+struct CBasis<float> {
+  static __device__ __forceinline__ float get(int k, int w, int idx) { return c_basis_f[k][w][idx]; }
+};
+
+template <int K, typename T = double>
+__device__ __forceinline__ T bS(int q, int i) { return CBasis<T>::get(K, 0, q * (K + 1) + i); }
+template <int K, typename T = double>
+__device__ __forceinline__ T bD(int q, int i) { return CBasis<T>::get(K, 1, q * (K + 1) + i); }
 
 struct SrcPtrs {
   const double *p[12];
@@ -53,42 +68,41 @@ __device__ __forceinline__ int face_node(int f, int i) {
 }
 
 // thread-dependent basis row (x = x_col) and column (node t) in registers
-template <int K>
-__device__ __forceinline__ void load_rows(int col, double (&Sx)[K + 1], double (&Dx)[K + 1]) {
+template <int K, typename T>
+__device__ __forceinline__ void load_rows(int col, T (&Sx)[K + 1], T (&Dx)[K + 1]) {
 #pragma unroll
   for (int i = 0; i <= K; ++i) {
-    Sx[i] = bS<K>(col, i);
-    Dx[i] = bD<K>(col, i);
+    Sx[i] = bS<K, T>(col, i);
+    Dx[i] = bD<K, T>(col, i);
   }
 }
-template <int K>
-__device__ __forceinline__ void load_cols(int t, double (&St)[2 * K + 1],
-                                          double (&Dt)[2 * K + 1]) {
+template <int K, typename T>
+__device__ __forceinline__ void load_cols(int t, T (&St)[2 * K + 1], T (&Dt)[2 * K + 1]) {
 #pragma unroll
   for (int q = 0; q < 2 * K + 1; ++q) {
-    St[q] = bS<K>(q, t);
-    Dt[q] = bD<K>(q, t);
+    St[q] = bS<K, T>(q, t);
+    Dt[q] = bD<K, T>(q, t);
   }
 }
 
 // values of a nodal tile on the thread's quadrature column
-template <int K>
-__device__ __forceinline__ void eval_col(const double *__restrict__ tile,
-                                         const double (&Sx)[K + 1], double (&v)[2 * K + 1]) {
+template <int K, typename T>
+__device__ __forceinline__ void eval_col(const T *__restrict__ tile, const T (&Sx)[K + 1],
+                                         T (&v)[2 * K + 1]) {
   constexpr int NN = K + 1, NQ = 2 * K + 1;
-  double t[NN];
+  T t[NN];
 #pragma unroll
   for (int iz = 0; iz < NN; ++iz) {
-    double s = 0.0;
+    T s = 0;
 #pragma unroll
     for (int ix = 0; ix < NN; ++ix) s = fma(Sx[ix], tile[iz * NN + ix], s);
     t[iz] = s;
   }
 #pragma unroll
   for (int qz = 0; qz < NQ; ++qz) {
-    double s = 0.0;
+    T s = 0;
 #pragma unroll
-    for (int iz = 0; iz < NN; ++iz) s = fma(bS<K>(qz, iz), t[iz], s);
+    for (int iz = 0; iz < NN; ++iz) s = fma(bS<K, T>(qz, iz), t[iz], s);
     v[qz] = s;
   }
 }
@@ -96,22 +110,20 @@ __device__ __forceinline__ void eval_col(const double *__restrict__ tile,
 // z-contraction of the submitted quantities of one column:
 //   xa[iz][col] = sum_qz S(qz,iz) V + D(qz,iz) Geta ;  xb[iz][col] = sum_qz S(qz,iz) Gxi
 // V, Gxi, Geta already carry JxW and the inverse Jacobian.
-template <int K, bool HAS_V, bool HAS_G>
-__device__ __forceinline__ void integrate_col_z(const double (&V)[2 * K + 1],
-                                                const double (&Gxi)[2 * K + 1],
-                                                const double (&Get)[2 * K + 1],
-                                                double *__restrict__ xa,
-                                                double *__restrict__ xb, int col) {
+template <int K, bool HAS_V, bool HAS_G, typename T>
+__device__ __forceinline__ void integrate_col_z(const T (&V)[2 * K + 1], const T (&Gxi)[2 * K + 1],
+                                                const T (&Get)[2 * K + 1], T *__restrict__ xa,
+                                                T *__restrict__ xb, int col) {
   constexpr int NN = K + 1, NQ = 2 * K + 1;
 #pragma unroll
   for (int iz = 0; iz < NN; ++iz) {
-    double sa = 0.0, sb = 0.0;
+    T sa = 0, sb = 0;
 #pragma unroll
     for (int qz = 0; qz < NQ; ++qz) {
-      if (HAS_V) sa = fma(bS<K>(qz, iz), V[qz], sa);
+      if (HAS_V) sa = fma(bS<K, T>(qz, iz), V[qz], sa);
       if (HAS_G) {
-        sa = fma(bD<K>(qz, iz), Get[qz], sa);
-        sb = fma(bS<K>(qz, iz), Gxi[qz], sb);
+        sa = fma(bD<K, T>(qz, iz), Get[qz], sa);
+        sb = fma(bS<K, T>(qz, iz), Gxi[qz], sb);
       }
     }
     xa[iz * NQ + col] = sa;
@@ -120,16 +132,14 @@ __device__ __forceinline__ void integrate_col_z(const double (&V)[2 * K + 1],
 }
 
 // x-contraction for output node column ix = t: out[iz] = sum_qx S(qx,t) xa + D(qx,t) xb
-template <int K, bool HAS_G>
-__device__ __forceinline__ void integrate_out(const double *__restrict__ xa,
-                                              const double *__restrict__ xb,
-                                              const double (&St)[2 * K + 1],
-                                              const double (&Dt)[2 * K + 1],
-                                              double (&out)[K + 1]) {
+template <int K, bool HAS_G, typename T>
+__device__ __forceinline__ void integrate_out(const T *__restrict__ xa, const T *__restrict__ xb,
+                                              const T (&St)[2 * K + 1], const T (&Dt)[2 * K + 1],
+                                              T (&out)[K + 1]) {
   constexpr int NN = K + 1, NQ = 2 * K + 1;
 #pragma unroll
   for (int iz = 0; iz < NN; ++iz) {
-    double s = 0.0;
+    T s = 0;
 #pragma unroll
     for (int qx = 0; qx < NQ; ++qx) {
       s = fma(St[qx], xa[iz * NQ + qx], s);
@@ -140,13 +150,12 @@ __device__ __forceinline__ void integrate_out(const double *__restrict__ xa,
 }
 
 // add the face contributions F[f][q] (JxW included) to output node column t
-template <int K>
-__device__ __forceinline__ void add_face_out(const double *__restrict__ F, int t,
-                                             const double (&St)[2 * K + 1],
-                                             double (&out)[K + 1]) {
+template <int K, typename T>
+__device__ __forceinline__ void add_face_out(const T *__restrict__ F, int t,
+                                             const T (&St)[2 * K + 1], T (&out)[K + 1]) {
   constexpr int NN = K + 1, NQ = 2 * K + 1;
   // faces z=0 / z=1: node (iz=0|K, ix=t)
-  double s2 = 0.0, s3 = 0.0;
+  T s2 = 0, s3 = 0;
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     s2 = fma(St[q], F[2 * NQ + q], s2);
@@ -156,22 +165,21 @@ __device__ __forceinline__ void add_face_out(const double *__restrict__ F, int t
   out[K] += s3;
   // faces x=0 / x=1: whole node column ix = 0 / ix = K
   if (t == 0 || t == K) {
-    const double *Ff = F + (t == 0 ? 0 : NQ);
+    const T *Ff = F + (t == 0 ? 0 : NQ);
 #pragma unroll
     for (int iz = 0; iz < NN; ++iz) {
-      double s = 0.0;
+      T s = 0;
 #pragma unroll
-      for (int q = 0; q < NQ; ++q) s = fma(bS<K>(q, iz), Ff[q], s);
+      for (int q = 0; q < NQ; ++q) s = fma(bS<K, T>(q, iz), Ff[q], s);
       out[iz] += s;
     }
   }
 }
 
 // trace of a nodal tile at face quadrature point `col` (row Sx = S[col][.])
-template <int K>
-__device__ __forceinline__ double face_val(const double *__restrict__ tile, int f,
-                                           const double (&Sx)[K + 1]) {
-  double s = 0.0;
+template <int K, typename T>
+__device__ __forceinline__ T face_val(const T *__restrict__ tile, int f, const T (&Sx)[K + 1]) {
+  T s = 0;
 #pragma unroll
   for (int i = 0; i <= K; ++i) s = fma(Sx[i], tile[face_node<K>(f, i)], s);
   return s;
@@ -179,13 +187,13 @@ __device__ __forceinline__ double face_val(const double *__restrict__ tile, int 
 
 // cooperative, coalesced copy of the block's cells of one field into tiles
 // dst tile slot = tiles[(lc*NT + t0 + comp)*NN2 + i]
-template <int K>
-__device__ __forceinline__ void load_tiles(double *__restrict__ tiles, int NT, int t0,
-                                           const double *__restrict__ src, int ncomp,
-                                           int c0, int cnt) {
+template <int K, typename T>
+__device__ __forceinline__ void load_tiles(T *__restrict__ tiles, int NT, int t0,
+                                           const T *__restrict__ src, int ncomp, int c0,
+                                           int cnt) {
   constexpr int NN2 = (K + 1) * (K + 1);
   const int per = ncomp * NN2;
-  const double *s = src + (long)c0 * per;
+  const T *s = src + (long)c0 * per;
   for (int e = threadIdx.x; e < cnt * per; e += blockDim.x) {
     const int lc = e / per;
     const int r = e - lc * per;
@@ -196,13 +204,15 @@ __device__ __forceinline__ void load_tiles(double *__restrict__ tiles, int NT, i
 }
 
 // physical gradient (gx, gz) at a quadrature point -> reference space * JxW
-struct QGeo {
-  double xx, xz, ex, ez, jxw;
+template <typename T>
+struct QGeoT {
+  T xx, xz, ex, ez, jxw;
 };
-template <int K>
-__device__ __forceinline__ QGeo qgeo(const double *__restrict__ g, int q) {
+using QGeo = QGeoT<double>;
+template <int K, typename T>
+__device__ __forceinline__ QGeoT<T> qgeo(const T *__restrict__ g, int q) {
   constexpr int NQ2 = (2 * K + 1) * (2 * K + 1);
-  QGeo r;
+  QGeoT<T> r;
   r.xx = g[q];
   r.xz = g[NQ2 + q];
   r.ex = g[2 * NQ2 + q];
@@ -211,10 +221,10 @@ __device__ __forceinline__ QGeo qgeo(const double *__restrict__ g, int q) {
   return r;
 }
 
-template <int K>
+template <int K, typename T = double>
 inline size_t smem_bytes(int n_tiles, int ncomp_out) {
   using C = Cfg<K>;
-  return sizeof(double) * (size_t)C::CPB *
+  return sizeof(T) * (size_t)C::CPB *
          ((size_t)n_tiles * C::NN2 + (size_t)ncomp_out * 2 * C::NN * C::NQ +
           (size_t)ncomp_out * 4 * C::NQ);
 }

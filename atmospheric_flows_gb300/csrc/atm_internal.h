@@ -25,6 +25,7 @@ struct Tableau {
 
 // Per-stage weights handed to the explicit-operator kernels.
 struct Solver;
+struct MG;
 
 struct StageCoef {
   double ca[3];  // explicit advection weights (a / b)
@@ -37,7 +38,7 @@ struct StageCoef {
 // Kernel families timed by the optional per-launch CUDA-event timers.
 enum KFam {
   KF_RHS_RHO = 0, KF_RHS_VEL, KF_RHS_PRES, KF_B, KF_CD, KF_MASS, KF_DIAG, KF_BLOCK_INV,
-  KF_BLOCK_APPLY, KF_COUNT
+  KF_BLOCK_APPLY, KF_MG_APPLY, KF_MG_OTHER, KF_COUNT
 };
 
 // CUDA-event timers around operator launches (off unless enabled).
@@ -55,15 +56,18 @@ struct KTimer {
 // Every kernel launch of the library increments this counter.
 extern std::atomic<long> g_kernel_launches;
 
-// Device geometry + connectivity of one mesh.
-struct Mesh {
+// Device geometry + connectivity of one mesh (T = double for the operator,
+// float for the multigrid levels of the mixed-precision preconditioner).
+template <typename T>
+struct MeshT {
   int nc = 0, k = 0, nn = 0, nq = 0, nn2 = 0, nq2 = 0;
-  double *qgeo = nullptr;  // [nc][5][nq2]: dxi/dx*JxW, dxi/dz*JxW, deta/dx*JxW, deta/dz*JxW, JxW
-  double *fgeo = nullptr;  // [nc][4][3][nq]: n_x, n_z, JxW (own-side, outward)
-  int *nbr = nullptr;      // [nc][4] neighbour cell, -1 at a wall
-  int *nbrf = nullptr;     // [nc][4] neighbour's local face index
-  double *minv = nullptr;  // [nc][nn2*nn2] inverse unit mass, stored transposed
+  T *qgeo = nullptr;   // [nc][5][nq2]: dxi/dx*JxW, dxi/dz*JxW, deta/dx*JxW, deta/dz*JxW, JxW
+  T *fgeo = nullptr;   // [nc][4][3][nq]: n_x, n_z, JxW (own-side, outward)
+  int *nbr = nullptr;  // [nc][4] neighbour cell, -1 at a wall
+  int *nbrf = nullptr; // [nc][4] neighbour's local face index
+  T *minv = nullptr;   // [nc][nn2*nn2] inverse unit mass, stored transposed
 };
+using Mesh = MeshT<double>;
 
 }  // namespace atm
 
@@ -90,6 +94,9 @@ struct atm_ctx {
   double *krylov = nullptr;
   double *dsmall = nullptr;  // device scratch for Hessenberg columns / y
   atm::Solver *solver = nullptr;
+  atm::MG *mg = nullptr;  // multigrid hierarchy of the FGMRES Schur solves
+  // GMRES/FGMRES only stop on a recomputed true residual (S is nonlinear)
+  bool true_residual_check = false;
   mutable atm::KTimer timer;
   long n_scalar() const { return (long)nc * nn2; }
   long n_vector() const { return 2L * nc * nn2; }
@@ -191,7 +198,47 @@ int vec_diagnostics(cudaStream_t st, const double *rho, const double *u, const d
 int vec_sponge(cudaStream_t st, double *u, const double *alpha, double dt, double ub0,
                double ub1, int nc, int nn2);
 
+// ------------------------------------------------------------- MG levels --
+// Operator data of one multigrid level (T = float: mixed precision; double:
+// the FP64 multigrid path).
+template <typename T>
+struct LevelViewT {
+  int k, nc;
+  MeshT<T> mesh;
+  const T *ainv;  // [nc][nn2*nn2] inverse rho_fix-weighted mass (transposed)
+  const T *invd;  // inverse diagonal of D
+  cudaStream_t st;
+};
+template <typename T>
+int level_B(const LevelViewT<T> &v, T *dst, const T *p, T cB, int mode);
+template <typename T>
+int level_CD(const LevelViewT<T> &v, T *dst, const T *w, const T *p, const T *pfix, T cC,
+             int mode);
+template <typename T>
+int level_inv_diag(const LevelViewT<T> &v, T *out, T scale);
+template <typename T>
+int level_block_inverse(const LevelViewT<T> &v, T *out, const T *weight);
+
+// multigrid hierarchy (mg.cu)
+int mg_add_level(atm_ctx &c, int n_cells, int mapdeg, const double *nodes, int n_inner,
+                 const int *inner, int n_bdry, const int *bdry, const int *children);
+int mg_free(atm_ctx &c);
+int mg_set_params(atm_ctx &c, int degree, double range, int eig_its, int coarse_degree);
+int mg_precondition(atm_ctx &c, int precision, double *z, const double *v);
+// precision 1: FP32 V-cycle, 2: FP64 V-cycle
+int fgmres_mg(atm_ctx &c, int precision, double *x, const double *b, double tol, int maxit,
+              int *its, double *res);
+void mg_mark_rho_changed(atm_ctx &c);
+long mg_vcycles(const atm_ctx &c);
+int mg_levels(const atm_ctx &c);
+
 // ------------------------------------------------------------ mesh set-up --
+struct HostMesh {
+  std::vector<double> qgeo, fgeo;
+  std::vector<int> nbr, nbrf;
+};
+int build_mesh_tables(int k, int nc, int mapdeg, const double *nodes, int n_inner,
+                      const int *inner, int n_bdry, const int *bdry, HostMesh &out);
 int mesh_upload(atm_ctx &c, int mapdeg, const double *nodes, int n_inner, const int *inner,
                 int n_bdry, const int *bdry);
 void mesh_free(Mesh &m);

@@ -87,6 +87,7 @@ static void ctx_free(atm_ctx *c) {
   cudaFree(c->krylov);
   cudaFree(c->dsmall);
   if (c->h_red) cudaFreeHost(c->h_red);
+  mg_free(*c);
   for (cudaEvent_t e : c->timer.ev) cudaEventDestroy(e);
   delete c;
 }
@@ -325,6 +326,45 @@ int atm_solve(atm_handle h, double *x, const double *b, double tol, int maxit, i
   return op_solve(*h, x, b, tol, maxit, iters, res);
 }
 
+// ------------------------------------------------------------- multigrid --
+int atm_mg_add_level(atm_handle h, int n_cells, int mapping_degree, const double *mapping_nodes,
+                     int n_inner, const int *inner_faces, int n_bdry, const int *bdry_faces,
+                     const int *children) {
+  CHECK_H(h);
+  return mg_add_level(*h, n_cells, mapping_degree, mapping_nodes, n_inner, inner_faces, n_bdry,
+                      bdry_faces, children);
+}
+int atm_mg_set_smoother(atm_handle h, int degree, double smoothing_range, int eig_iterations,
+                        int coarse_degree) {
+  CHECK_H(h);
+  return mg_set_params(*h, degree, smoothing_range, eig_iterations, coarse_degree);
+}
+int atm_mg_vcycle(atm_handle h, int precision, double *dst, const double *src) {
+  CHECK_H(h);
+  CHECK_PTR(dst, "dst");
+  CHECK_PTR(src, "src");
+  if (precision != 1 && precision != 2) { set_error("precision must be 1 or 2"); return ATM_BAD_ARG; }
+  return mg_precondition(*h, precision, dst, src);
+}
+int atm_set_true_residual_check(atm_handle h, int on) {
+  CHECK_H(h);
+  h->true_residual_check = on != 0;
+  return ATM_OK;
+}
+int atm_solve_fgmres(atm_handle h, int precision, double *x, const double *b, double tol,
+                     int maxit, int *iters, double *res) {
+  CHECK_H(h);
+  CHECK_PTR(x, "x");
+  CHECK_PTR(b, "b");
+  if (maxit < 0 || !(tol >= 0.0)) { set_error("bad tolerance or maxit"); return ATM_BAD_ARG; }
+  int it = 0;
+  double r = 0.0;
+  int rc = fgmres_mg(*h, precision, x, b, tol, maxit, &it, &r);
+  if (iters) *iters = it;
+  if (res) *res = r;
+  return rc;
+}
+
 // ----------------------------------------------------------------- solver --
 int atm_solver_init(atm_handle h, double dt, double mach, double froude, double eps,
                     int max_its, int precision) {
@@ -333,9 +373,14 @@ int atm_solver_init(atm_handle h, double dt, double mach, double froude, double 
     set_error("atm_solver_init: dt, Mach, Froude, eps must be positive, max_its >= 1");
     return ATM_BAD_ARG;
   }
-  if (precision != 0) {
-    set_error("atm_solver_init: precision mode not available in this build");
+  if (precision < 0 || precision > 2) {
+    set_error("atm_solver_init: precision must be 0 (GMRES + Jacobi), 1 (FGMRES + FP32 "
+              "multigrid) or 2 (FGMRES + FP64 multigrid)");
     return ATM_BAD_ARG;
+  }
+  if (precision > 0 && mg_levels(*h) < 2) {
+    set_error("atm_solver_init: precision 1/2 needs multigrid levels (atm_mg_add_level)");
+    return ATM_NOT_READY;
   }
   if (h->solver) {
     solver_free(*h->solver);
@@ -433,6 +478,7 @@ int atm_solver_stats(atm_handle h, double *st) {
   st[5] = (double)v.failures;
   st[6] = v.time;
   st[7] = h->dt;
+  st[8] = (double)mg_vcycles(*h);
   return ATM_OK;
 }
 int atm_solver_diagnostics(atm_handle h, double *out) {

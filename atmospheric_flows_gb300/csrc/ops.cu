@@ -63,7 +63,10 @@ static int read_small(atm_ctx &c, const double *dev, int n) {
   return ATM_OK;
 }
 
-int rebuild_ainv(atm_ctx &c) { return launch_block_inverse(c, c.ainv, c.rho_fix); }
+int rebuild_ainv(atm_ctx &c) {
+  mg_mark_rho_changed(c);
+  return launch_block_inverse(c, c.ainv, c.rho_fix);
+}
 
 // S p = D p - C A^{-1} B p  (euler_operator.h:2374-2408); with `precondition`
 // the result is multiplied by the inverse diagonal of D (PreconditionJacobi
@@ -187,7 +190,10 @@ int gmres_schur(atm_ctx &c, double *x, const double *b, double tol, int maxit, i
     // y lives in pageable host memory: make sure the copy finished before
     // the vector is reused
     ATM_CUDA(cudaStreamSynchronize(c.stream));
-    if (done) return (*res <= tol) ? ATM_OK : (*its >= maxit ? ATM_NOT_CONVERGED : ATM_OK);
+    // with the true-residual check a converged estimate only ends the cycle:
+    // the restart recomputes b - S(x) and decides
+    if (done && !c.true_residual_check)
+      return (*res <= tol) ? ATM_OK : (*its >= maxit ? ATM_NOT_CONVERGED : ATM_OK);
   }
 }
 

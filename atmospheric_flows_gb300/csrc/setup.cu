@@ -134,15 +134,17 @@ void mesh_free(Mesh &m) {
   m.nbr = m.nbrf = nullptr;
 }
 
-int mesh_upload(atm_ctx &c, int mapdeg, const double *nodes, int n_inner, const int *inner,
-                int n_bdry, const int *bdry) {
-  const int k = c.k, nn = k + 1, nq = 2 * k + 1, nq2 = nq * nq, nc = c.nc;
+int build_mesh_tables(int k, int nc, int mapdeg, const double *nodes, int n_inner,
+                      const int *inner, int n_bdry, const int *bdry, HostMesh &out) {
+  const int nq = 2 * k + 1, nq2 = nq * nq;
   if (mapdeg < 1 || mapdeg > 8 || !nodes || (n_inner > 0 && !inner) || (n_bdry > 0 && !bdry)) {
-    set_error("atm_upload_mesh: bad mapping degree or null table");
+    set_error("mesh tables: bad mapping degree or null table");
     return ATM_BAD_ARG;
   }
   // --- connectivity
-  std::vector<int> nbr((size_t)nc * 4, -2), nbrf((size_t)nc * 4, -1);
+  std::vector<int> &nbr = out.nbr, &nbrf = out.nbrf;
+  nbr.assign((size_t)nc * 4, -2);
+  nbrf.assign((size_t)nc * 4, -1);
   for (int f = 0; f < n_inner; ++f) {
     const int *e = inner + 5L * f;
     if (e[0] < 0 || e[0] >= nc || e[2] < 0 || e[2] >= nc || e[1] < 0 || e[1] > 3 ||
@@ -195,7 +197,9 @@ int mesh_upload(atm_ctx &c, int mapdeg, const double *nodes, int n_inner, const 
   std::vector<double> L0, dL0, L1, dL1;
   tab(0.0, L0, dL0);
   tab(1.0, L1, dL1);
-  std::vector<double> qgeo((size_t)nc * 5 * nq2), fgeo((size_t)nc * 4 * 3 * nq);
+  std::vector<double> &qgeo = out.qgeo, &fgeo = out.fgeo;
+  qgeo.assign((size_t)nc * 5 * nq2, 0.0);
+  fgeo.assign((size_t)nc * 4 * 3 * nq, 0.0);
   // J = [[dx/dxi, dx/deta],[dz/dxi, dz/deta]] at (La, dLa) x (Lb, dLb)
   auto jac = [&](int cell, const double *La, const double *dLa, const double *Lb,
                  const double *dLb, double J[4]) {
@@ -250,20 +254,29 @@ int mesh_upload(atm_ctx &c, int mapdeg, const double *nodes, int n_inner, const 
         fgeo[base + 2 * nq + q] = det * len * b.weights[q];
       }
   }
+  return ATM_OK;
+}
+
+int mesh_upload(atm_ctx &c, int mapdeg, const double *nodes, int n_inner, const int *inner,
+                int n_bdry, const int *bdry) {
+  HostMesh hm;
+  int rc = build_mesh_tables(c.k, c.nc, mapdeg, nodes, n_inner, inner, n_bdry, bdry, hm);
+  if (rc) return rc;
+  const int k = c.k, nn = k + 1, nq = 2 * k + 1, nq2 = nq * nq, nc = c.nc;
   mesh_free(c.mesh);
   Mesh &m = c.mesh;
   m.nc = nc; m.k = k; m.nn = nn; m.nq = nq; m.nn2 = nn * nn; m.nq2 = nq2;
-  ATM_CUDA(cudaMalloc(&m.qgeo, qgeo.size() * sizeof(double)));
-  ATM_CUDA(cudaMalloc(&m.fgeo, fgeo.size() * sizeof(double)));
-  ATM_CUDA(cudaMalloc(&m.nbr, nbr.size() * sizeof(int)));
-  ATM_CUDA(cudaMalloc(&m.nbrf, nbrf.size() * sizeof(int)));
+  ATM_CUDA(cudaMalloc(&m.qgeo, hm.qgeo.size() * sizeof(double)));
+  ATM_CUDA(cudaMalloc(&m.fgeo, hm.fgeo.size() * sizeof(double)));
+  ATM_CUDA(cudaMalloc(&m.nbr, hm.nbr.size() * sizeof(int)));
+  ATM_CUDA(cudaMalloc(&m.nbrf, hm.nbrf.size() * sizeof(int)));
   ATM_CUDA(cudaMalloc(&m.minv, (size_t)nc * m.nn2 * m.nn2 * sizeof(double)));
-  ATM_CUDA(cudaMemcpy(m.qgeo, qgeo.data(), qgeo.size() * sizeof(double), cudaMemcpyHostToDevice));
-  ATM_CUDA(cudaMemcpy(m.fgeo, fgeo.data(), fgeo.size() * sizeof(double), cudaMemcpyHostToDevice));
-  ATM_CUDA(cudaMemcpy(m.nbr, nbr.data(), nbr.size() * sizeof(int), cudaMemcpyHostToDevice));
-  ATM_CUDA(cudaMemcpy(m.nbrf, nbrf.data(), nbrf.size() * sizeof(int), cudaMemcpyHostToDevice));
+  ATM_CUDA(cudaMemcpy(m.qgeo, hm.qgeo.data(), hm.qgeo.size() * sizeof(double), cudaMemcpyHostToDevice));
+  ATM_CUDA(cudaMemcpy(m.fgeo, hm.fgeo.data(), hm.fgeo.size() * sizeof(double), cudaMemcpyHostToDevice));
+  ATM_CUDA(cudaMemcpy(m.nbr, hm.nbr.data(), hm.nbr.size() * sizeof(int), cudaMemcpyHostToDevice));
+  ATM_CUDA(cudaMemcpy(m.nbrf, hm.nbrf.data(), hm.nbrf.size() * sizeof(int), cudaMemcpyHostToDevice));
   c.mapdeg = mapdeg;
-  int rc = launch_block_inverse(c, m.minv, nullptr);
+  rc = launch_block_inverse(c, m.minv, nullptr);
   if (rc) return rc;
   rc = launch_inv_diag(c, c.invdiag_D, 1, nullptr, 1.0 / (GAS_GAMMA - 1.0));
   if (rc) return rc;

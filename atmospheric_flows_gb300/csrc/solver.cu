@@ -98,7 +98,9 @@ int pressure_fixed_point(atm_ctx &c, Solver &s) {
   TRY(vec_copy(c.stream, s.pres_fixed, s.pres_fixed_old, ns));
   int its = 0;
   double res = 0.0;
-  int rc = gmres_schur(c, s.pres_fixed, s.rhs_pres, tol, s.max_its, &its, &res);
+  int rc = s.precision == 0
+               ? gmres_schur(c, s.pres_fixed, s.rhs_pres, tol, s.max_its, &its, &res)
+               : fgmres_mg(c, s.precision, s.pres_fixed, s.rhs_pres, tol, s.max_its, &its, &res);
   s.krylov_total += its;
   if (rc == ATM_NOT_CONVERGED) { ++s.failures; rc = ATM_OK; }
   return rc;

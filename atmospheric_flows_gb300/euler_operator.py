@@ -164,5 +164,36 @@ class EULEROperator:
             _lib.check(code, "atm_solve")
         return code, its.value, res.value
 
+    # ------------------------------------------- mixed-precision multigrid --
+    def add_mg_level(self, level):
+        """Add the next coarser level (dict from ``hill.mg_hierarchy``)."""
+        nodes, pn = _np_d(level["mapping_nodes"])
+        inner, pi = _np_i(level["inner_faces"])
+        bdry, pb = _np_i(level["boundary_faces"])
+        ch, pc = _np_i(level["children"])
+        _lib.call("atm_mg_add_level", self._h, int(level["n_cells"]),
+                  self.storage.mapping_degree, pn, len(inner), pi, len(bdry), pb, pc)
+
+    def set_mg_smoother(self, degree=3, smoothing_range=15.0, eig_iterations=10,
+                        coarse_degree=20):
+        _lib.call("atm_mg_set_smoother", self._h, int(degree), float(smoothing_range),
+                  int(eig_iterations), int(coarse_degree))
+
+    def mg_vcycle(self, dst, src, precision=1):
+        """One V-cycle, FP32 (precision 1) or FP64 (precision 2)."""
+        _lib.call("atm_mg_vcycle", self._h, int(precision), _ptr(dst), _ptr(src))
+
+    def set_true_residual_check(self, on):
+        _lib.call("atm_set_true_residual_check", self._h, int(bool(on)))
+
+    def solve_fgmres(self, x, b, tol, maxit=30000, precision=1):
+        its = ctypes.c_int(0)
+        res = ctypes.c_double(0.0)
+        code = _lib.load().atm_solve_fgmres(self._h, int(precision), _ptr(x), _ptr(b), float(tol),
+                                            int(maxit), ctypes.byref(its), ctypes.byref(res))
+        if code not in (0, 2):
+            _lib.check(code, "atm_solve_fgmres")
+        return code, its.value, res.value
+
     def synchronize(self):
         _lib.call("atm_synchronize", self._h)

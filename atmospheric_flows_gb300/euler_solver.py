@@ -24,13 +24,22 @@ def _d(a):
 class EulerSolver:
     """IMEX-DG solver for one member (one device context)."""
 
-    PRECISION_FP64 = 0
-    PRECISION_MIXED = 1
+    REFERENCE_SOLVER = 0  # GMRES + Jacobi on diag(D), as the reference
+    PRECISION_MIXED = 1   # FGMRES + FP32 multigrid V-cycle
+    PRECISION_FP64_MG = 2  # FGMRES + FP64 multigrid V-cycle
 
-    def __init__(self, case, eps=1e-8, max_its=30000, precision=0, dt=None):
+    def __init__(self, case, eps=1e-8, max_its=30000, precision=0, dt=None, mg_levels=8,
+                 true_residual_check=False):
         self.case = case
         self.op = EULEROperator(MatrixFreeStorage.from_case(case))
         self.dt = case.dt if dt is None else float(dt)
+        self.precision = int(precision)
+        self.op.set_true_residual_check(true_residual_check)
+        if self.precision in (self.PRECISION_MIXED, self.PRECISION_FP64_MG):
+            from .hill import mg_hierarchy
+
+            for level in mg_hierarchy(case.params, max_levels=mg_levels):
+                self.op.add_mg_level(level)
         _lib.call("atm_solver_init", self.op.handle, self.dt, case.Ma, case.Fr, float(eps),
                   int(max_its), int(precision))
         self.n_scalar = self.op.n_scalar
@@ -53,10 +62,10 @@ class EulerSolver:
         _lib.call("atm_solver_run", self.op.handle, int(n_steps))
 
     def stats(self):
-        s = np.zeros(8)
+        s = np.zeros(9)
         _lib.call("atm_solver_stats", self.op.handle, _d(s))
         keys = ("steps", "picard_total", "krylov_total", "picard_stage1", "picard_stage2",
-                "solve_fail", "time", "dt")
+                "solve_fail", "time", "dt", "vcycles")
         return dict(zip(keys, s.tolist()))
 
     def diagnostics(self):

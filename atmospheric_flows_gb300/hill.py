@@ -218,3 +218,30 @@ def build_case(p: HillParams | None = None, **kw) -> HillCase:
                     u=np.ascontiguousarray(u.reshape(-1)),
                     p=np.ascontiguousarray(p_nd), sponge_alpha=alpha.reshape(-1),
                     dt=dt)
+
+
+def mg_hierarchy(p: HillParams, max_levels: int = 8, min_cells_z: int = 1):
+    """Coarse levels for the FP32 multigrid preconditioner.
+
+    Returns a list of dicts (fine to coarse, level 1 first) with the mesh
+    tables of the (nx/2^l) x (nz/2^l) mesh and ``children[n_cells][4]``: the
+    level l-1 cells at positions (x-,z-), (x+,z-), (x-,z+), (x+,z+)."""
+    levels = []
+    nx, nz = p.nx, p.nz
+    while (len(levels) + 1 < max_levels and nx % 2 == 0 and nz % 2 == 0
+           and nz // 2 >= min_cells_z and nx // 2 >= 1):
+        nxc, nzc = nx // 2, nz // 2
+        pc = dataclasses.replace(p, nx=nxc, nz=nzc)
+        nodes, inner, bdry = build_mesh(pc)
+        ch = np.empty((nxc * nzc, 4), dtype=np.int32)
+        for iz in range(nzc):
+            for ix in range(nxc):
+                c = iz * nxc + ix
+                for b in range(2):
+                    for a in range(2):
+                        ch[c, a + 2 * b] = (2 * iz + b) * nx + 2 * ix + a
+        levels.append(dict(n_cells=nxc * nzc, mapping_nodes=np.ascontiguousarray(nodes),
+                           inner_faces=inner, boundary_faces=bdry, children=ch,
+                           nx=nxc, nz=nzc))
+        nx, nz = nxc, nzc
+    return levels

@@ -74,8 +74,10 @@ long atm_n_scalar(atm_handle h);
  * 249).  atm_kernel_launches counts every kernel launch of the library in
  * this process.  With timing enabled, each operator launch is bracketed by
  * CUDA events on the context's stream; atm_timing_read synchronises and
- * returns, per family 0..8 = rhs_rho, rhs_vel, rhs_pres, B, C/D, mass,
- * diagonal, block inverse, block apply: total ms, launches, algorithmic HBM
+ * returns, per family 0..10 = rhs_rho, rhs_vel, rhs_pres, B, C/D, mass,
+ * diagonal, block inverse, block apply, multigrid level Schur apply (B+C/D
+ * pair, any level), whole V-cycle (nested: contains the level applies):
+ * total ms, launches, algorithmic HBM
  * bytes (fields read + written, 8 B per node value) and FP64 flops of the
  * sum-factorisation contractions; then resets them.  Any output may be NULL. */
 long atm_kernel_launches(void);
@@ -156,14 +158,46 @@ int atm_solve(atm_handle h, double *x, const double *b, double tol, int maxit,
               int *iters, double *res);
 
 /* ---------------------------------------------------------------------------
+ * Mixed-precision Schur solve: FP64 flexible GMRES right-preconditioned by an
+ * FP32 geometric-multigrid V-cycle with Chebyshev smoothing (the reference's
+ * smoother recipe, Atmospheric_Flow.cc:489-502, applied to the Schur system,
+ * which the reference solves with GMRES + Jacobi, Atmospheric_Flow.cc:656-672).
+ * Levels are added fine to coarse.  Level 0 is the context's mesh.  Each call
+ * adds the next coarser mesh, whose cells are unions of 2x2 cells of the
+ * previous level: children[n_cells][4] lists, for each coarse cell, the
+ * previous-level cells at positions (x-,z-), (x+,z-), (x-,z+), (x+,z+).
+ * Mesh tables as in atm_ctx_create. */
+int atm_mg_add_level(atm_handle h, int n_cells, int mapping_degree, const double *mapping_nodes,
+                     int n_inner, const int *inner_faces, int n_bdry, const int *bdry_faces,
+                     const int *children);
+/* Chebyshev degree (3), smoothing range (15), power iterations for the
+ * largest eigenvalue (10), degree of the coarsest-level Chebyshev (20). */
+int atm_mg_set_smoother(atm_handle h, int degree, double smoothing_range, int eig_iterations,
+                        int coarse_degree);
+/* One V-cycle: dst ~= S^{-1} src (FP64 device vectors); precision 1 runs the
+ * V-cycle in FP32, 2 in FP64. */
+int atm_mg_vcycle(atm_handle h, int precision, double *dst, const double *src);
+/* FGMRES(16) + V-cycle on S x = b (NS 2 operator state); tol absolute on the
+ * unpreconditioned residual; precision as for atm_mg_vcycle. */
+int atm_solve_fgmres(atm_handle h, int precision, double *x, const double *b, double tol,
+                     int maxit, int *iters, double *res);
+/* S is not linear (the upwind lambda of C depends on A^{-1}B p,
+ * euler_operator.h:1497-1498), so a Krylov solve that stops on its
+ * linearised residual estimate returns an answer that depends on the Krylov
+ * algorithm.  With this option on, GMRES and FGMRES only stop on the
+ * recomputed true residual b - S(x).  Off (default) = deal.II SolverGMRES. */
+int atm_set_true_residual_check(atm_handle h, int on);
+
+/* ---------------------------------------------------------------------------
  * Time loop.  Replaces EulerSolver (Atmospheric_Flow.cc:57-272,1100-1257):
  * the 3-stage IMEX step with the Picard loop (<= 100 iterations, 1e-10
  * relative L-infinity stop), stage combination and an optional Rayleigh
  * sponge on u (applied after stage 3).  The solver state lives in the
  * context (one solver per context); set/get use HOST pointers unless the
  * name ends in _device.
- *   precision: 0 = FP64 GMRES + Jacobi (the reference solver),
- *              1 = FP64 flexible GMRES with an FP32 multigrid preconditioner.
+ *   precision: 0 = FP64 GMRES + Jacobi on diag(D) (the reference solver),
+ *              1 = FP64 flexible GMRES + FP32 multigrid V-cycle,
+ *              2 = FP64 flexible GMRES + FP64 multigrid V-cycle.
  * ------------------------------------------------------------------------- */
 int atm_solver_init(atm_handle h, double dt, double mach, double froude, double eps,
                     int max_its, int precision);
@@ -177,9 +211,9 @@ int atm_solver_get_state_device(atm_handle h, double *rho, double *u, double *p)
 int atm_solver_set_sponge(atm_handle h, const double *alpha_nodes, double ubg_x,
                           double ubg_z);
 int atm_solver_run(atm_handle h, int n_steps);
-/* stats[0..7] as doubles: steps, Picard iterations (total), Krylov
+/* stats[0..8] as doubles: steps, Picard iterations (total), Krylov
  * iterations (total), last Picard count stage 1, stage 2, Krylov solves that
- * hit max_its, simulated time, current dt. */
+ * hit max_its, simulated time, current dt, V-cycles (total). */
 int atm_solver_stats(atm_handle h, double *stats);
 /* Diagnostics of Atmospheric_Flow.cc:991-1087 at the Gauss-Lobatto nodes:
  * out[0..3] = min rho, max |rho|, max sqrt(gamma p/rho), max |u|. */

@@ -61,6 +61,9 @@ def lib():
                                         ctypes.c_int]
         L.orc_solver_destroy.argtypes = [ctypes.c_void_p]
         L.orc_solver_set_inner_tol.argtypes = [ctypes.c_void_p, ctypes.c_double]
+        L.orc_solver_set_true_residual_check.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_set_true_residual_check.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_solver_set_schur_tol_preconditioned.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_solver_set_state.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
         L.orc_solver_get_state.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
         L.orc_solver_set_sponge.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double,
@@ -118,6 +121,9 @@ class OracleOperator:
 
     def set_inner_tol(self, tol):
         lib().orc_set_inner_tol(self.h, tol)
+
+    def set_true_residual_check(self, on):
+        lib().orc_set_true_residual_check(self.h, int(bool(on)))
 
     def set_rho_for_fixed(self, v):
         v = np.ascontiguousarray(v, dtype=np.float64)
@@ -194,7 +200,8 @@ class OracleOperator:
 class OracleSolver:
     """CPU restatement of ``EulerSolver`` (Atmospheric_Flow.cc:57-1257)."""
 
-    def __init__(self, case, eps=1e-8, max_its=30000, inner_tol=1e-12, dt=None):
+    def __init__(self, case, eps=1e-8, max_its=30000, inner_tol=1e-12, dt=None,
+                 true_residual_check=False, schur_tol_preconditioned=False):
         L = lib()
         self.case = case
         self._nodes = np.ascontiguousarray(case.mapping_nodes, dtype=np.float64)
@@ -206,6 +213,8 @@ class OracleSolver:
                                      case.dt if dt is None else dt, case.Ma, case.Fr, eps,
                                      max_its)
         L.orc_solver_set_inner_tol(self.h, inner_tol)
+        L.orc_solver_set_true_residual_check(self.h, int(bool(true_residual_check)))
+        L.orc_solver_set_schur_tol_preconditioned(self.h, int(bool(schur_tol_preconditioned)))
         self.set_state(case.rho, case.u, case.p)
         alpha = np.ascontiguousarray(case.sponge_alpha, dtype=np.float64)
         L.orc_solver_set_sponge(self.h, _d(alpha), case.params.u0, 0.0)
