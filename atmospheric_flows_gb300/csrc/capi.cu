@@ -155,6 +155,8 @@ int atm_ctx_destroy(atm_handle h) {
 int atm_upload_mesh(atm_handle h, int mapping_degree, const double *mapping_nodes, int n_inner,
                     const int *inner_faces, int n_bdry, const int *bdry_faces) {
   CHECK_H(h);
+  // a multigrid hierarchy built on the old mesh no longer matches
+  mg_free(*h);
   return mesh_upload(*h, mapping_degree, mapping_nodes, n_inner, inner_faces, n_bdry,
                      bdry_faces);
 }

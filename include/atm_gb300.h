@@ -60,7 +60,8 @@ int atm_ctx_create(int dim, int degree, int n_cells, int mapping_degree,
                    const double *mapping_nodes, int n_inner, const int *inner_faces,
                    int n_bdry, const int *bdry_faces, atm_handle *out);
 int atm_ctx_destroy(atm_handle h);
-/* Re-upload geometry and connectivity after mesh adaptation (same sizes). */
+/* Re-upload geometry and connectivity after mesh adaptation (same sizes).
+ * Drops the multigrid levels: add them again for the new mesh. */
 int atm_upload_mesh(atm_handle h, int mapping_degree, const double *mapping_nodes,
                     int n_inner, const int *inner_faces, int n_bdry,
                     const int *bdry_faces);
