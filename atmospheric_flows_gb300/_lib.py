@@ -26,6 +26,9 @@ SIGNATURES = {
     "atm_upload_mesh": (_i, [_h, _i, _dp, _i, _ip, _i, _ip]),
     "atm_set_stream": (_i, [_h, ctypes.c_void_p]),
     "atm_synchronize": (_i, [_h]),
+    "atm_stream_create": (_i, [ctypes.POINTER(ctypes.c_void_p)]),
+    "atm_stream_destroy": (_i, [ctypes.c_void_p]),
+    "atm_device_memory": (_i, [_dp, _dp]),
     "atm_n_scalar": (ctypes.c_long, [_h]),
     "atm_kernel_launches": (ctypes.c_long, []),
     "atm_probe_fma_peak": (_i, [_dp, _dp]),
@@ -59,6 +62,7 @@ SIGNATURES = {
     "atm_solver_set_state_device": (_i, [_h, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "atm_solver_get_state_device": (_i, [_h, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "atm_solver_set_sponge": (_i, [_h, _dp, _d, _d]),
+    "atm_solver_set_clock": (_i, [_h, _d, ctypes.c_long]),
     "atm_solver_run": (_i, [_h, _i]),
     "atm_solver_stats": (_i, [_h, _dp]),
     "atm_solver_diagnostics": (_i, [_h, _dp]),

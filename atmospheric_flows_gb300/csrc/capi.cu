@@ -120,7 +120,7 @@ int atm_ctx_create(int dim, int degree, int n_cells, int mapping_degree,
   do {                                                                         \
     cudaError_t e = cudaMalloc(&(ptr), (size_t)(n) * sizeof(double));          \
     if (e != cudaSuccess) return fail(cuda_fail(e, "cudaMalloc " #ptr));       \
-    cudaMemset((ptr), 0, (size_t)(n) * sizeof(double));                        \
+    cudaMemsetAsync((ptr), 0, (size_t)(n) * sizeof(double), c->stream);         \
   } while (0)
   ALLOC(c->rho_fix, ns);
   ALLOC(c->pres_fix, ns);
@@ -164,6 +164,24 @@ int atm_upload_mesh(atm_handle h, int mapping_degree, const double *mapping_node
 int atm_set_stream(atm_handle h, void *stream) {
   CHECK_H(h);
   h->stream = static_cast<cudaStream_t>(stream);
+  return ATM_OK;
+}
+int atm_stream_create(void **out) {
+  CHECK_PTR(out, "out");
+  cudaStream_t s = nullptr;
+  ATM_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  *out = s;
+  return ATM_OK;
+}
+int atm_stream_destroy(void *stream) {
+  if (stream) ATM_CUDA(cudaStreamDestroy(static_cast<cudaStream_t>(stream)));
+  return ATM_OK;
+}
+int atm_device_memory(double *free_bytes, double *total_bytes) {
+  size_t f = 0, t = 0;
+  ATM_CUDA(cudaMemGetInfo(&f, &t));
+  if (free_bytes) *free_bytes = (double)f;
+  if (total_bytes) *total_bytes = (double)t;
   return ATM_OK;
 }
 int atm_synchronize(atm_handle h) {
@@ -455,6 +473,13 @@ int atm_solver_set_sponge(atm_handle h, const double *alpha, double ubg_x, doubl
   v.sponge = true;
   v.ubg0 = ubg_x;
   v.ubg1 = ubg_z;
+  return ATM_OK;
+}
+int atm_solver_set_clock(atm_handle h, double time, long steps) {
+  CHECK_S(h);
+  if (steps < 0 || !(time >= 0.0)) { set_error("time and steps must be >= 0"); return ATM_BAD_ARG; }
+  h->solver->time = time;
+  h->solver->steps = steps;
   return ATM_OK;
 }
 int atm_solver_run(atm_handle h, int n_steps) {

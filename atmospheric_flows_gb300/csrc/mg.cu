@@ -298,14 +298,14 @@ int level_alloc(atm_ctx &c, MGLevelT<T> &L, const HostMesh &hm) {
   ATM_CUDA(cudaMalloc(&L.mesh.fgeo, ff.size() * sizeof(T)));
   ATM_CUDA(cudaMalloc(&L.mesh.nbr, hm.nbr.size() * sizeof(int)));
   ATM_CUDA(cudaMalloc(&L.mesh.nbrf, hm.nbrf.size() * sizeof(int)));
-  ATM_CUDA(cudaMemcpy(L.mesh.qgeo, qf.data(), qf.size() * sizeof(T), cudaMemcpyHostToDevice));
-  ATM_CUDA(cudaMemcpy(L.mesh.fgeo, ff.data(), ff.size() * sizeof(T), cudaMemcpyHostToDevice));
-  ATM_CUDA(cudaMemcpy(L.mesh.nbr, hm.nbr.data(), hm.nbr.size() * sizeof(int), cudaMemcpyHostToDevice));
-  ATM_CUDA(cudaMemcpy(L.mesh.nbrf, hm.nbrf.data(), hm.nbrf.size() * sizeof(int), cudaMemcpyHostToDevice));
+  ATM_CUDA(cudaMemcpyAsync(L.mesh.qgeo, qf.data(), qf.size() * sizeof(T), cudaMemcpyHostToDevice, c.stream));
+  ATM_CUDA(cudaMemcpyAsync(L.mesh.fgeo, ff.data(), ff.size() * sizeof(T), cudaMemcpyHostToDevice, c.stream));
+  ATM_CUDA(cudaMemcpyAsync(L.mesh.nbr, hm.nbr.data(), hm.nbr.size() * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+  ATM_CUDA(cudaMemcpyAsync(L.mesh.nbrf, hm.nbrf.data(), hm.nbrf.size() * sizeof(int), cudaMemcpyHostToDevice, c.stream));
   T **vecs[] = {&L.invd, &L.rho, &L.pfix, &L.x, &L.b, &L.r, &L.t, &L.d};
   for (T **v : vecs) {
     ATM_CUDA(cudaMalloc(v, ns * sizeof(T)));
-    ATM_CUDA(cudaMemset(*v, 0, ns * sizeof(T)));
+    ATM_CUDA(cudaMemsetAsync(*v, 0, ns * sizeof(T), c.stream));
   }
   ATM_CUDA(cudaMalloc(&L.wv, 2 * ns * sizeof(T)));
   ATM_CUDA(cudaMalloc(&L.ainv, (size_t)L.nc * nn2 * nn2 * sizeof(T)));
@@ -335,10 +335,10 @@ int build_hier(atm_ctx &c, MG &mg) {
       ATM_CUDA(cudaMalloc(&F.parent, F.nc * sizeof(int)));
       ATM_CUDA(cudaMalloc(&F.ppos, F.nc * sizeof(int)));
       ATM_CUDA(cudaMalloc(&H.lv[l].children, ch.size() * sizeof(int)));
-      ATM_CUDA(cudaMemcpy(F.parent, parent.data(), F.nc * sizeof(int), cudaMemcpyHostToDevice));
-      ATM_CUDA(cudaMemcpy(F.ppos, ppos.data(), F.nc * sizeof(int), cudaMemcpyHostToDevice));
-      ATM_CUDA(cudaMemcpy(H.lv[l].children, ch.data(), ch.size() * sizeof(int),
-                          cudaMemcpyHostToDevice));
+      ATM_CUDA(cudaMemcpyAsync(F.parent, parent.data(), F.nc * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+      ATM_CUDA(cudaMemcpyAsync(F.ppos, ppos.data(), F.nc * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+      ATM_CUDA(cudaMemcpyAsync(H.lv[l].children, ch.data(), ch.size() * sizeof(int),
+                               cudaMemcpyHostToDevice, c.stream));
     }
   }
   H.built = true;
@@ -545,10 +545,11 @@ int mg_add_level(atm_ctx &c, int n_cells, int mapdeg, const double *nodes, int n
     hm.fgeo.resize((size_t)c.nc * 4 * 3 * c.nq);
     hm.nbr.resize((size_t)c.nc * 4);
     hm.nbrf.resize((size_t)c.nc * 4);
-    ATM_CUDA(cudaMemcpy(hm.qgeo.data(), c.mesh.qgeo, hm.qgeo.size() * 8, cudaMemcpyDeviceToHost));
-    ATM_CUDA(cudaMemcpy(hm.fgeo.data(), c.mesh.fgeo, hm.fgeo.size() * 8, cudaMemcpyDeviceToHost));
-    ATM_CUDA(cudaMemcpy(hm.nbr.data(), c.mesh.nbr, hm.nbr.size() * 4, cudaMemcpyDeviceToHost));
-    ATM_CUDA(cudaMemcpy(hm.nbrf.data(), c.mesh.nbrf, hm.nbrf.size() * 4, cudaMemcpyDeviceToHost));
+    ATM_CUDA(cudaMemcpyAsync(hm.qgeo.data(), c.mesh.qgeo, hm.qgeo.size() * 8, cudaMemcpyDeviceToHost, c.stream));
+    ATM_CUDA(cudaMemcpyAsync(hm.fgeo.data(), c.mesh.fgeo, hm.fgeo.size() * 8, cudaMemcpyDeviceToHost, c.stream));
+    ATM_CUDA(cudaMemcpyAsync(hm.nbr.data(), c.mesh.nbr, hm.nbr.size() * 4, cudaMemcpyDeviceToHost, c.stream));
+    ATM_CUDA(cudaMemcpyAsync(hm.nbrf.data(), c.mesh.nbrf, hm.nbrf.size() * 4, cudaMemcpyDeviceToHost, c.stream));
+    ATM_CUDA(cudaStreamSynchronize(c.stream));
     mg->hm.push_back(std::move(hm));
     mg->ncells.push_back(c.nc);
     mg->children.emplace_back();

@@ -271,10 +271,10 @@ int mesh_upload(atm_ctx &c, int mapdeg, const double *nodes, int n_inner, const 
   ATM_CUDA(cudaMalloc(&m.nbr, hm.nbr.size() * sizeof(int)));
   ATM_CUDA(cudaMalloc(&m.nbrf, hm.nbrf.size() * sizeof(int)));
   ATM_CUDA(cudaMalloc(&m.minv, (size_t)nc * m.nn2 * m.nn2 * sizeof(double)));
-  ATM_CUDA(cudaMemcpy(m.qgeo, hm.qgeo.data(), hm.qgeo.size() * sizeof(double), cudaMemcpyHostToDevice));
-  ATM_CUDA(cudaMemcpy(m.fgeo, hm.fgeo.data(), hm.fgeo.size() * sizeof(double), cudaMemcpyHostToDevice));
-  ATM_CUDA(cudaMemcpy(m.nbr, hm.nbr.data(), hm.nbr.size() * sizeof(int), cudaMemcpyHostToDevice));
-  ATM_CUDA(cudaMemcpy(m.nbrf, hm.nbrf.data(), hm.nbrf.size() * sizeof(int), cudaMemcpyHostToDevice));
+  ATM_CUDA(cudaMemcpyAsync(m.qgeo, hm.qgeo.data(), hm.qgeo.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+  ATM_CUDA(cudaMemcpyAsync(m.fgeo, hm.fgeo.data(), hm.fgeo.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+  ATM_CUDA(cudaMemcpyAsync(m.nbr, hm.nbr.data(), hm.nbr.size() * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+  ATM_CUDA(cudaMemcpyAsync(m.nbrf, hm.nbrf.data(), hm.nbrf.size() * sizeof(int), cudaMemcpyHostToDevice, c.stream));
   c.mapdeg = mapdeg;
   rc = launch_block_inverse(c, m.minv, nullptr);
   if (rc) return rc;

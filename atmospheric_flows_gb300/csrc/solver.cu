@@ -22,7 +22,8 @@ int solver_alloc(atm_ctx &c, Solver &s) {
   const long ns = c.n_scalar(), nv = c.n_vector();
   const long total = 12 * ns + 7 * nv;
   ATM_CUDA(cudaMalloc(&s.pool, total * sizeof(double)));
-  ATM_CUDA(cudaMemset(s.pool, 0, total * sizeof(double)));
+  ATM_CUDA(cudaMemsetAsync(s.pool, 0, total * sizeof(double), c.stream));
+  ATM_CUDA(cudaStreamSynchronize(c.stream));
   double *p = s.pool;
   auto take = [&](long n) { double *r = p; p += n; return r; };
   s.rho_old = take(ns); s.rho_tmp_2 = take(ns); s.rho_tmp_3 = take(ns);

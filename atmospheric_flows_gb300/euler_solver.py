@@ -29,9 +29,12 @@ class EulerSolver:
     PRECISION_FP64_MG = 2  # FGMRES + FP64 multigrid V-cycle
 
     def __init__(self, case, eps=1e-8, max_its=30000, precision=0, dt=None, mg_levels=8,
-                 true_residual_check=False):
+                 true_residual_check=False, stream=None):
         self.case = case
         self.op = EULEROperator(MatrixFreeStorage.from_case(case))
+        self.stream = stream
+        if stream is not None:
+            _lib.call("atm_set_stream", self.op.handle, ctypes.c_void_p(stream))
         self.dt = case.dt if dt is None else float(dt)
         self.precision = int(precision)
         self.op.set_true_residual_check(true_residual_check)
@@ -72,6 +75,29 @@ class EulerSolver:
         out = np.zeros(4)
         _lib.call("atm_solver_diagnostics", self.op.handle, _d(out))
         return dict(zip(("min_rho", "max_rho", "max_celerity", "max_velocity"), out.tolist()))
+
+    # ------------------------------------------------- checkpoint / restart --
+    def save(self, path):
+        """Write the state, clock and case parameters to ``path`` (.npz).
+
+        The reference only writes VTU output for visualisation
+        (Atmospheric_Flow.cc:885-918); this is a restartable raw dump."""
+        import dataclasses
+
+        rho, u, p = self.get_state()
+        st = self.stats()
+        np.savez(path, rho=rho, u=u, p=p, time=st["time"], steps=int(st["steps"]),
+                 dt=self.dt, precision=self.precision,
+                 params=np.array(repr(dataclasses.asdict(self.case.params))))
+
+    def load(self, path):
+        """Restore a state written by :meth:`save` (same case and mesh)."""
+        d = np.load(path)
+        n = self.n_scalar
+        if d["rho"].shape != (n,) or d["u"].shape != (2 * n,):
+            raise ValueError("checkpoint does not match this member's mesh/degree")
+        self.set_state(d["rho"], d["u"], d["p"])
+        _lib.call("atm_solver_set_clock", self.op.handle, float(d["time"]), int(d["steps"]))
 
     def close(self):
         self.op.close()

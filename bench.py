@@ -56,6 +56,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--only-headline", action="store_true",
                     help="skip the multigrid variants (short runs, profiling)")
+    ap.add_argument("--serving", action="store_true",
+                    help="run a bounded sample of the ensemble-serving workload and exit")
+    ap.add_argument("--serving-requests", type=int, default=48)
+    ap.add_argument("--serving-rate", type=float, default=8.0)
+    ap.add_argument("--serving-steps-scale", type=float, default=0.05)
     ap.add_argument("--fma-probe", action="store_true",
                     help="print the measured FP64/FP32 FMA peaks and exit")
     return ap.parse_args()
@@ -385,10 +390,36 @@ def fma_probe():
     return 0
 
 
+def serving(args):
+    """Ensemble-serving sample: Poisson arrivals, mesh/degree/parameter
+    draws of the serving workload, continuous batching under an HBM budget."""
+    import torch
+
+    torch.cuda.set_device(0)
+    from atmospheric_flows_gb300.serving import Server, make_requests, summarize
+
+    reqs = make_requests(n=args.serving_requests, rate=args.serving_rate, seed=0,
+                         steps_scale=args.serving_steps_scale)
+    srv = Server(hbm_budget=150e9, max_running=32)
+    res = srv.run(reqs)
+    s = summarize(res, srv.makespan)
+    s.update({"metric": "ensemble serving latency / aggregate DoF-steps/s", "unit": "s",
+              "requests_sample": f"{args.serving_requests} requests, Poisson rate "
+                                 f"{args.serving_rate}/s, steps 100-400 scaled by "
+                                 f"{args.serving_steps_scale}, meshes 40x20..320x160, k 2-5",
+              "hbm_budget_gb": 150, "peak_running": srv.peak_running,
+              "peak_reserved_gb": srv.peak_bytes / 1e9,
+              "solver": "FP64 state, FGMRES + FP32 multigrid, rtol 1e-8 true residual"})
+    print(json.dumps(s), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.fma_probe:
         return fma_probe()
+    if args.serving:
+        return serving(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gb300(args)

@@ -68,6 +68,13 @@ int atm_upload_mesh(atm_handle h, int mapping_degree, const double *mapping_node
 /* cudaStream_t as void*; NULL = the legacy default stream. */
 int atm_set_stream(atm_handle h, void *stream);
 int atm_synchronize(atm_handle h);
+/* A non-blocking CUDA stream (as void*) for one member of an ensemble, so
+ * that members driven from different host threads overlap on the device
+ * (no reference counterpart: the reference runs one member per MPI job). */
+int atm_stream_create(void **out);
+int atm_stream_destroy(void *stream);
+/* cudaMemGetInfo of the current device, for admission against a budget. */
+int atm_device_memory(double *free_bytes, double *total_bytes);
 /* Sizes: scalar field length n_cells*(k+1)^2; velocity twice that. */
 long atm_n_scalar(atm_handle h);
 
@@ -211,6 +218,8 @@ int atm_solver_set_state_device(atm_handle h, const double *rho, const double *u
 int atm_solver_get_state_device(atm_handle h, double *rho, double *u, double *p);
 int atm_solver_set_sponge(atm_handle h, const double *alpha_nodes, double ubg_x,
                           double ubg_z);
+/* Restore the simulated time and step count (checkpoint restart). */
+int atm_solver_set_clock(atm_handle h, double time, long steps);
 int atm_solver_run(atm_handle h, int n_steps);
 /* stats[0..8] as doubles: steps, Picard iterations (total), Krylov
  * iterations (total), last Picard count stage 1, stage 2, Krylov solves that

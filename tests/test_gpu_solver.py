@@ -70,3 +70,21 @@ def test_mass_conservation_gpu(cuda_ok):
     assert abs(op.vmult(rho).sum() - m0) / m0 < 1e-12
     d = g.diagnostics()
     assert d["min_rho"] > 0 and np.isfinite(d["max_velocity"])
+
+
+def test_checkpoint_restart_is_exact(cuda_ok, tmp_path):
+    from atmospheric_flows_gb300.euler_solver import EulerSolver
+
+    case = build_case(HillParams(nx=8, nz=4, degree=3, cfl=3.0))
+    a = EulerSolver(case, eps=1e-10)
+    a.run(2)
+    path = str(tmp_path / "member.npz")
+    a.save(path)
+    a.run(2)
+    ref = a.get_state()
+    b = EulerSolver(case, eps=1e-10)
+    b.load(path)
+    assert b.stats()["steps"] == 2
+    b.run(2)
+    for x, y in zip(b.get_state(), ref):
+        assert np.array_equal(x, y)
