@@ -151,6 +151,10 @@ def measured_peaks():
 # FP64 FMA throughput of this machine's GB300 (1255 GFLOP/s measured with an
 # independent-chain DFMA probe; profiles/fp64_fp32_fma_peak.md)
 FP64_PEAK_TFLOPS = 1.255
+# DRAM bytes (read + write) per cell and launch of the dominant kernel families,
+# from `ncu` captures of this bench at 320x160 (profiles/k_CD_q4_320x160.md);
+# the traffic grows in proportion to the cell count.
+NCU_TRAFFIC_PER_CELL = {4: {"CD": 273.1e6 / 51200}}
 
 
 def cpu_baseline(case, eps):
@@ -338,6 +342,9 @@ def run_gb300(args):
     tflops = flp[dom] / max(cnt[dom], 1) / (avg_ms * 1e-3) / 1e12
     peak, peak_kind = measured_peaks()
     traffic = os.environ.get("ATM_NCU_TRAFFIC_BYTES")
+    if traffic is None and args.degree in NCU_TRAFFIC_PER_CELL and \
+            fams[dom] in NCU_TRAFFIC_PER_CELL[args.degree]:
+        traffic = NCU_TRAFFIC_PER_CELL[args.degree][fams[dom]] * case.n_cells
     total_ms = sum(ms[i] for i in cand)
     roofline = {"bound": "hbm", "kernel": fams[dom], "achieved": gbs, "peak": peak,
                 "unit": "GB/s", "frac": gbs / peak, "peak_source": peak_kind,
