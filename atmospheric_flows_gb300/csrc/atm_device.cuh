@@ -28,14 +28,17 @@ struct Cfg {
   static constexpr int THREADS = CPB * NQ;
 };
 
-// [degree][0: values, 1: derivatives][q*(k+1)+i] at the 2k+1 Gauss points.
-// Each translation unit holds its own copy in its constant bank.
-static __constant__ double c_basis[KMAX + 1][2][NQ_MAX * NN_MAX];
-static __constant__ float c_basis_f[KMAX + 1][2][NQ_MAX * NN_MAX];
+// [degree][w][q*(k+1)+i]: w = 0 values and 1 derivatives at the 2k+1 Gauss
+// points g_q; w = 2, 3 values at the subface points (g_q + s)/2, s = 0, 1, of
+// a hanging face.  Each translation unit holds its own copy in its constant
+// bank.
+constexpr int BASIS_TABLES = 4;
+static __constant__ double c_basis[KMAX + 1][BASIS_TABLES][NQ_MAX * NN_MAX];
+static __constant__ float c_basis_f[KMAX + 1][BASIS_TABLES][NQ_MAX * NN_MAX];
 
 static inline int upload_basis_here(const double *table) {
-  float tf[(KMAX + 1) * 2 * NQ_MAX * NN_MAX];
-  for (int i = 0; i < (KMAX + 1) * 2 * NQ_MAX * NN_MAX; ++i) tf[i] = (float)table[i];
+  float tf[(KMAX + 1) * BASIS_TABLES * NQ_MAX * NN_MAX];
+  for (int i = 0; i < (KMAX + 1) * BASIS_TABLES * NQ_MAX * NN_MAX; ++i) tf[i] = (float)table[i];
   if (cudaMemcpyToSymbol(c_basis, table, sizeof(c_basis)) != cudaSuccess) return 1;
   return cudaMemcpyToSymbol(c_basis_f, tf, sizeof(c_basis_f)) == cudaSuccess ? 0 : 1;
 }
@@ -55,6 +58,11 @@ template <int K, typename T = double>
 __device__ __forceinline__ T bS(int q, int i) { return CBasis<T>::get(K, 0, q * (K + 1) + i); }
 template <int K, typename T = double>
 __device__ __forceinline__ T bD(int q, int i) { return CBasis<T>::get(K, 1, q * (K + 1) + i); }
+// value of basis function i at point q of subface s of a hanging face
+template <int K, typename T = double>
+__device__ __forceinline__ T bH(int s, int q, int i) {
+  return CBasis<T>::get(K, 2 + s, q * (K + 1) + i);
+}
 
 struct SrcPtrs {
   const double *p[12];
@@ -176,6 +184,115 @@ __device__ __forceinline__ void add_face_out(const T *__restrict__ F, int t,
   }
 }
 
+// Face contributions with hanging faces: like add_face_out, but on a face of
+// code 3 (this cell is the coarse side, bit f of hmask) the two subface
+// fluxes F (s = 0) and Fh (s = 1) are integrated against the shifted basis.
+template <int K, typename T>
+__device__ __forceinline__ void add_face_out_hg(const T *__restrict__ F, const T *__restrict__ Fh,
+                                                int hmask, int t, const T (&St)[2 * K + 1],
+                                                T (&out)[K + 1]) {
+  if (hmask == 0) {
+    add_face_out<K>(F, t, St, out);
+    return;
+  }
+  constexpr int NN = K + 1, NQ = 2 * K + 1;
+#pragma unroll
+  for (int f = 2; f < 4; ++f) {
+    T s = 0;
+    if ((hmask >> f) & 1) {
+      for (int q = 0; q < NQ; ++q)
+        s = fma(bH<K, T>(0, q, t), F[f * NQ + q], fma(bH<K, T>(1, q, t), Fh[f * NQ + q], s));
+    } else {
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) s = fma(St[q], F[f * NQ + q], s);
+    }
+    out[f == 2 ? 0 : K] += s;
+  }
+  if (t == 0 || t == K) {
+    const int f = t == 0 ? 0 : 1;
+    const bool hang = (hmask >> f) & 1;
+#pragma unroll
+    for (int iz = 0; iz < NN; ++iz) {
+      T s = 0;
+      if (hang) {
+        for (int q = 0; q < NQ; ++q)
+          s = fma(bH<K, T>(0, q, iz), F[f * NQ + q], fma(bH<K, T>(1, q, iz), Fh[f * NQ + q], s));
+      } else {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) s = fma(bS<K, T>(q, iz), F[f * NQ + q], s);
+      }
+      out[iz] += s;
+    }
+  }
+}
+
+// bit f set when face f of cell c is the coarse side of a hanging face
+template <typename T>
+__device__ __forceinline__ int hanging_mask(const MeshT<T> &mesh, int c) {
+  int m = 0;
+#pragma unroll
+  for (int f = 0; f < 4; ++f)
+    if (mesh.nbr[c * 4 + f] >= 0 && (mesh.nbrf[c * 4 + f] >> 2) == 3) m |= 1 << f;
+  return m;
+}
+
+// Walks the four faces of cell c for the column thread `col` and calls
+//   body(f, nb, nf, n0, n1, jxw, Ro, Rn, val)
+// once per face point: nb/nf the neighbour cell and its local face (nb < 0 at a
+// wall), (n0, n1, jxw) the outward normal and the face weight, Ro / Rn the
+// basis rows giving this cell's and the neighbour's trace at the point.  The
+// body returns NC face values in val, stored at fbc[comp*4*NQ + f*NQ + col].
+// With HG, a face of code 1/2 reads the neighbour at the shifted points; a face
+// of code 3 is integrated on its two subfaces, with the s = 1 values going to
+// fhc (same layout).  Without HG the loop is the conforming one.
+template <int K, int NC, bool HG, typename T, typename Body>
+__device__ __forceinline__ void face_terms(const MeshT<T> &mesh, int c, int col,
+                                           const T (&Sx)[K + 1], T *__restrict__ fbc,
+                                           T *__restrict__ fhc, Body &&body) {
+  constexpr int NQ = 2 * K + 1;
+  for (int f = 0; f < 4; ++f) {
+    const int nb = mesh.nbr[c * 4 + f];
+    const int nfc = mesh.nbrf[c * 4 + f];
+    const int code = HG && nb >= 0 ? (nfc >> 2) : 0;
+    T val[NC];
+    if (code == 0) {
+      const T *fg = mesh.fgeo + ((long)c * 4 + f) * 3 * NQ;
+      body(f, nb, nfc & 3, fg[col], fg[NQ + col], fg[2 * NQ + col], Sx, Sx, val);
+#pragma unroll
+      for (int comp = 0; comp < NC; ++comp) fbc[comp * 4 * NQ + f * NQ + col] = val[comp];
+    } else if (code < 3) {
+      const T *fg = mesh.fgeo + ((long)c * 4 + f) * 3 * NQ;
+      T Rn[K + 1];
+#pragma unroll
+      for (int i = 0; i <= K; ++i) Rn[i] = bH<K, T>(code - 1, col, i);
+      body(f, nb, nfc & 3, fg[col], fg[NQ + col], fg[2 * NQ + col], Sx, Rn, val);
+#pragma unroll
+      for (int comp = 0; comp < NC; ++comp) fbc[comp * 4 * NQ + f * NQ + col] = val[comp];
+    } else {
+      for (int s = 0; s < 2; ++s) {
+        const T *hg = mesh.hgeo + ((long)nb * 2 + s) * 3 * NQ;
+        T Ro[K + 1];
+#pragma unroll
+        for (int i = 0; i <= K; ++i) Ro[i] = bH<K, T>(s, col, i);
+        body(f, mesh.hnb[nb * 2 + s], nfc & 3, hg[col], hg[NQ + col], hg[2 * NQ + col], Ro, Sx,
+             val);
+        T *o = s == 0 ? fbc : fhc;
+#pragma unroll
+        for (int comp = 0; comp < NC; ++comp) o[comp * 4 * NQ + f * NQ + col] = val[comp];
+      }
+    }
+  }
+}
+
+// add the face values of the output column t (conforming or with hanging faces)
+template <int K, bool HG, typename T>
+__device__ __forceinline__ void add_faces(const MeshT<T> &mesh, int c, const T *__restrict__ F,
+                                          const T *__restrict__ Fh, int t,
+                                          const T (&St)[2 * K + 1], T (&out)[K + 1]) {
+  if (HG) add_face_out_hg<K>(F, Fh, hanging_mask(mesh, c), t, St, out);
+  else add_face_out<K>(F, t, St, out);
+}
+
 // trace of a nodal tile at face quadrature point `col` (row Sx = S[col][.])
 template <int K, typename T>
 __device__ __forceinline__ T face_val(const T *__restrict__ tile, int f, const T (&Sx)[K + 1]) {
@@ -221,12 +338,13 @@ __device__ __forceinline__ QGeoT<T> qgeo(const T *__restrict__ g, int q) {
   return r;
 }
 
+// tiles, x-contraction exchange, face values [, subface-1 face values]
 template <int K, typename T = double>
-inline size_t smem_bytes(int n_tiles, int ncomp_out) {
+inline size_t smem_bytes(int n_tiles, int ncomp_out, bool hg = false) {
   using C = Cfg<K>;
   return sizeof(T) * (size_t)C::CPB *
          ((size_t)n_tiles * C::NN2 + (size_t)ncomp_out * 2 * C::NN * C::NQ +
-          (size_t)ncomp_out * 4 * C::NQ);
+          (size_t)ncomp_out * 4 * C::NQ * (hg ? 2 : 1));
 }
 
 }  // namespace atm

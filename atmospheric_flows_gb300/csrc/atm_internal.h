@@ -63,9 +63,18 @@ struct MeshT {
   int nc = 0, k = 0, nn = 0, nq = 0, nn2 = 0, nq2 = 0;
   T *qgeo = nullptr;   // [nc][5][nq2]: dxi/dx*JxW, dxi/dz*JxW, deta/dx*JxW, deta/dz*JxW, JxW
   T *fgeo = nullptr;   // [nc][4][3][nq]: n_x, n_z, JxW (own-side, outward)
-  int *nbr = nullptr;  // [nc][4] neighbour cell, -1 at a wall
-  int *nbrf = nullptr; // [nc][4] neighbour's local face index
+  int *nbr = nullptr;  // [nc][4] neighbour cell, -1 at a wall (hanging index h, code 3)
+  int *nbrf = nullptr; // [nc][4] neighbour's local face | code << 2 (see below)
   T *minv = nullptr;   // [nc][nn2*nn2] inverse unit mass, stored transposed
+  // Hanging faces of 2:1 adaptive meshes.  Code of a cell face (nbrf >> 2):
+  //   0 conforming; 1, 2: this cell is the fine side and its face is subface
+  //   code-1 of the neighbour's face; 3: this cell is the coarse side, nbr
+  //   holds the hanging-face index h, hnb[2h+s] is the fine neighbour on
+  //   subface s and hgeo[2h+s][3][nq] the subface geometry (n_x, n_z, JxW)
+  //   seen from this cell at the points (gauss_q + s)/2 of its face.
+  int nhang = 0;
+  int *hnb = nullptr;
+  T *hgeo = nullptr;
 };
 using Mesh = MeshT<double>;
 
@@ -236,6 +245,9 @@ int mg_levels(const atm_ctx &c);
 struct HostMesh {
   std::vector<double> qgeo, fgeo;
   std::vector<int> nbr, nbrf;
+  std::vector<int> hnb;      // [nhang][2]
+  std::vector<double> hgeo;  // [nhang][2][3][nq]
+  int nhang = 0;
 };
 int build_mesh_tables(int k, int nc, int mapdeg, const double *nodes, int n_inner,
                       const int *inner, int n_bdry, const int *bdry, HostMesh &out);

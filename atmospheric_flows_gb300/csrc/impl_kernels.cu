@@ -11,206 +11,16 @@
 // per cell instead of the reference's CG iterations (euler_operator.h:2391-2397,
 // Atmospheric_Flow.cc:452-536); the Schur apply S p = D p - C A^{-1} B p is
 // then two fused kernels: (B, A^{-1}) and (C, D, Jacobi).
-#include "atm_device.cuh"
+#include "schur_kernels.cuh"
 
 namespace atm {
 
 int upload_basis_impl(const double *t) { return upload_basis_here(t); }
 
-// ====================================================================== B ===
-// MODE 0: dst = B p ; 1: dst -= B p ; 2: dst = A^{-1} B p
-template <int K, int MODE, typename T>
-__global__ void __launch_bounds__(Cfg<K>::THREADS)
-    k_B(T *__restrict__ dst, const T *__restrict__ p, T cB,
-        const T *__restrict__ ainv, MeshT<T> mesh) {
-  using C = Cfg<K>;
-  constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2, CPB = C::CPB;
-  constexpr int NT = 1;
-  extern __shared__ __align__(16) unsigned char sm_raw[];
-  T *sm = reinterpret_cast<T *>(sm_raw);
-  T *tiles = sm;
-  T *xab = tiles + CPB * NT * NN2;  // [CPB][2][2][NN*NQ]
-  T *fb = xab + CPB * 4 * NN * NQ;  // [CPB][2][4][NQ]
-  T *bt = fb + CPB * 8 * NQ;        // [CPB][2][NN2] (MODE 2)
-  const int tid = threadIdx.x, lc = tid / NQ, col = tid - lc * NQ;
-  const int c0 = blockIdx.x * CPB;
-  const int cnt = min(CPB, mesh.nc - c0);
-  load_tiles<K>(tiles, NT, 0, p, 1, c0, cnt);
-  __syncthreads();
-  const bool active = lc < cnt;
-  const int c = c0 + lc;
-  T Sx[NN], Dx[NN];
-  load_rows<K>(col, Sx, Dx);
-  if (active) {
-    const T *tl = tiles + lc * NT * NN2;
-    T pv[NQ];
-    eval_col<K>(tl, Sx, pv);
-    const T *G = mesh.qgeo + (long)c * 5 * NQ2;
-    T V[NQ], Gxi[NQ], Get[NQ];
-    // submit_divergence(-cB p): component d is tested with d(phi)/dx_d
-#pragma unroll
-    for (int comp = 0; comp < 2; ++comp) {
-#pragma unroll
-      for (int qz = 0; qz < NQ; ++qz) {
-        const auto g = qgeo<K>(G, qz * NQ + col);
-        const T s = -cB * pv[qz];
-        Gxi[qz] = (comp == 0 ? g.xx : g.xz) * s;
-        Get[qz] = (comp == 0 ? g.ex : g.ez) * s;
-        V[qz] = T(0.0);
-      }
-      T *xa = xab + (lc * 2 + comp) * 2 * NN * NQ;
-      integrate_col_z<K, false, true>(V, Gxi, Get, xa, xa + NN * NQ, col);
-    }
-    for (int f = 0; f < 4; ++f) {
-      const int nb = mesh.nbr[c * 4 + f];
-      const T *fg = mesh.fgeo + ((long)c * 4 + f) * 3 * NQ;
-      const T n0 = fg[col], n1 = fg[NQ + col], jxw = fg[2 * NQ + col];
-      const T pp = face_val<K>(tl, f, Sx);
-      T avg;
-      if (nb >= 0) {
-        const T pm = face_val<K>(p + (long)nb * NN2, mesh.nbrf[c * 4 + f], Sx);
-        avg = T(0.5) * (pp + pm);
-      } else {
-        avg = T(0.5) * (pp + pp);  // wall, p_D = p
-      }
-      fb[((lc * 2 + 0) * 4 + f) * NQ + col] = cB * avg * n0 * jxw;
-      fb[((lc * 2 + 1) * 4 + f) * NQ + col] = cB * avg * n1 * jxw;
-    }
-  }
-  __syncthreads();
-  if (active && col < NN) {
-    T St[NQ], Dt[NQ];
-    load_cols<K>(col, St, Dt);
-#pragma unroll
-    for (int comp = 0; comp < 2; ++comp) {
-      T out[NN];
-      const T *xa = xab + (lc * 2 + comp) * 2 * NN * NQ;
-      integrate_out<K, true>(xa, xa + NN * NQ, St, Dt, out);
-      add_face_out<K>(fb + (lc * 2 + comp) * 4 * NQ, col, St, out);
-      if (MODE == 2) {
-#pragma unroll
-        for (int iz = 0; iz < NN; ++iz) bt[(lc * 2 + comp) * NN2 + iz * NN + col] = out[iz];
-      } else {
-        T *d = dst + ((long)c * 2 + comp) * NN2;
-#pragma unroll
-        for (int iz = 0; iz < NN; ++iz) {
-          if (MODE == 0) d[iz * NN + col] = out[iz];
-          else d[iz * NN + col] -= out[iz];
-        }
-      }
-    }
-  }
-  if (MODE == 2) {
-    __syncthreads();
-    if (active) {
-      const T *Ab = ainv + (long)c * NN2 * NN2;
-      const T *b0 = bt + (lc * 2 + 0) * NN2, *b1 = bt + (lc * 2 + 1) * NN2;
-      for (int i = col; i < NN2; i += NQ) {
-        T s0 = T(0.0), s1 = T(0.0);
-#pragma unroll 5
-        for (int j = 0; j < NN2; ++j) {
-          const T a = Ab[j * NN2 + i];  // transposed storage
-          s0 = fma(a, b0[j], s0);
-          s1 = fma(a, b1[j], s1);
-        }
-        dst[((long)c * 2 + 0) * NN2 + i] = s0;
-        dst[((long)c * 2 + 1) * NN2 + i] = s1;
-      }
-    }
-  }
-}
-
-// ===================================================================== CD ===
-// MODE 0: dst = C w ; 1: dst = sD D p - C w ; 2: dst = invd .* (sD D p - C w)
-// MODE 3: dst -= C w
-template <int K, int MODE, typename T>
-__global__ void __launch_bounds__(Cfg<K>::THREADS)
-    k_CD(T *__restrict__ dst, const T *__restrict__ w, const T *__restrict__ p,
-         const T *__restrict__ pfix, T cC, const T *__restrict__ invd,
-         MeshT<T> mesh) {
-  using C = Cfg<K>;
-  constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2, CPB = C::CPB;
-  constexpr bool WITH_D = (MODE == 1 || MODE == 2);
-  constexpr int NT = WITH_D ? 4 : 3;  // w(2), pfix, [p]
-  constexpr T GM1 = GAS_GAMMA - T(1.0);
-  constexpr T HG = GAS_GAMMA / (GAS_GAMMA - T(1.0));
-  // sign of the C contribution in dst
-  constexpr T SC = WITH_D ? -T(1.0) : T(1.0);
-  extern __shared__ __align__(16) unsigned char sm_raw[];
-  T *sm = reinterpret_cast<T *>(sm_raw);
-  T *tiles = sm;
-  T *xab = tiles + CPB * NT * NN2;
-  T *fb = xab + CPB * 2 * NN * NQ;
-  const int tid = threadIdx.x, lc = tid / NQ, col = tid - lc * NQ;
-  const int c0 = blockIdx.x * CPB;
-  const int cnt = min(CPB, mesh.nc - c0);
-  load_tiles<K>(tiles, NT, 0, w, 2, c0, cnt);
-  load_tiles<K>(tiles, NT, 2, pfix, 1, c0, cnt);
-  if (WITH_D) load_tiles<K>(tiles, NT, 3, p, 1, c0, cnt);
-  __syncthreads();
-  const bool active = lc < cnt;
-  const int c = c0 + lc;
-  T Sx[NN], Dx[NN];
-  load_rows<K>(col, Sx, Dx);
-  if (active) {
-    const T *tl = tiles + lc * NT * NN2;
-    T wx[NQ], wz[NQ], pf[NQ], pv[NQ];
-    eval_col<K>(tl, Sx, wx);
-    eval_col<K>(tl + NN2, Sx, wz);
-    eval_col<K>(tl + 2 * NN2, Sx, pf);
-    if (WITH_D) eval_col<K>(tl + 3 * NN2, Sx, pv);
-    const T *G = mesh.qgeo + (long)c * 5 * NQ2;
-    T V[NQ], Gxi[NQ], Get[NQ];
-#pragma unroll
-    for (int qz = 0; qz < NQ; ++qz) {
-      const auto g = qgeo<K>(G, qz * NQ + col);
-      // C: submit_gradient(-cC hg pfix w)
-      const T gx = SC * (-cC * HG * pf[qz] * wx[qz]);
-      const T gz = SC * (-cC * HG * pf[qz] * wz[qz]);
-      Gxi[qz] = g.xx * gx + g.xz * gz;
-      Get[qz] = g.ex * gx + g.ez * gz;
-      V[qz] = WITH_D ? (T(1.0) / GM1) * pv[qz] * g.jxw : T(0.0);
-    }
-    T *xa = xab + lc * 2 * NN * NQ;
-    integrate_col_z<K, WITH_D, true>(V, Gxi, Get, xa, xa + NN * NQ, col);
-    for (int f = 0; f < 4; ++f) {
-      const int nb = mesh.nbr[c * 4 + f];
-      T val = T(0.0);
-      if (nb >= 0) {
-        const int nf = mesh.nbrf[c * 4 + f];
-        const T *fg = mesh.fgeo + ((long)c * 4 + f) * 3 * NQ;
-        const T n0 = fg[col], n1 = fg[NQ + col], jxw = fg[2 * NQ + col];
-        const T wxp = face_val<K>(tl, f, Sx), wzp = face_val<K>(tl + NN2, f, Sx);
-        const T pfp = face_val<K>(tl + 2 * NN2, f, Sx);
-        const T wxm = face_val<K>(w + (long)nb * 2 * NN2, nf, Sx);
-        const T wzm = face_val<K>(w + ((long)nb * 2 + 1) * NN2, nf, Sx);
-        const T pfm = face_val<K>(pfix + (long)nb * NN2, nf, Sx);
-        const T av0 = T(0.5) * HG * (pfp * wxp + pfm * wxm);
-        const T av1 = T(0.5) * HG * (pfp * wzp + pfm * wzm);
-        const T lam = fmax(fabs(wxp * n0 + wzp * n1), fabs(wxm * n0 + wzm * n1));
-        const T je = T(1.0) / GM1 * (pfp - pfm);
-        val = SC * cC * ((av0 * n0 + av1 * n1) + T(0.5) * lam * je) * jxw;
-      }
-      fb[(lc * 4 + f) * NQ + col] = val;
-    }
-  }
-  __syncthreads();
-  if (active && col < NN) {
-    T St[NQ], Dt[NQ], out[NN];
-    load_cols<K>(col, St, Dt);
-    const T *xa = xab + lc * 2 * NN * NQ;
-    integrate_out<K, true>(xa, xa + NN * NQ, St, Dt, out);
-    add_face_out<K>(fb + lc * 4 * NQ, col, St, out);
-    T *d = dst + (long)c * NN2;
-#pragma unroll
-    for (int iz = 0; iz < NN; ++iz) {
-      const int i = iz * NN + col;
-      if (MODE == 2) d[i] = invd[(long)c * NN2 + i] * out[iz];
-      else if (MODE == 3) d[i] -= out[iz];
-      else d[i] = out[iz];
-    }
-  }
-}
+// hanging-face instantiations of B and C/D live in hang_kernels.cu
+int launch_B_hang(const atm_ctx &c, double *dst, const double *p, double coeff, int mode);
+int launch_CD_hang(const atm_ctx &c, double *dst, const double *w, const double *p,
+                   const double *pfix, double coeff, int mode);
 
 // ============================================================ mass apply ===
 // dst = M_w src for NCOMP components; weight tile (rho) or constant scale
@@ -414,49 +224,7 @@ __global__ void k_block_apply(T *__restrict__ dst, const T *__restrict__ src,
   }
 }
 
-// ============================================================ launchers ===
 namespace {
-template <typename T>
-struct OpView {
-  int k, nc;
-  MeshT<T> mesh;
-  const T *ainv;
-  const T *invd;
-  cudaStream_t st;
-};
-
-OpView<double> view(const atm_ctx &c) {
-  return OpView<double>{c.k, c.nc, c.mesh, c.ainv, c.invdiag_D, c.stream};
-}
-
-template <int K, typename T>
-int B_launch(const OpView<T> &v, T *dst, const T *p, T cB, int mode) {
-  using C = Cfg<K>;
-  const int grid = (v.nc + C::CPB - 1) / C::CPB;
-  const size_t sm = smem_bytes<K, T>(1, 2) + sizeof(T) * C::CPB * 2 * C::NN2;
-  if (mode == 0) k_B<K, 0, T><<<grid, C::THREADS, sm, v.st>>>(dst, p, cB, v.ainv, v.mesh);
-  else if (mode == 1) k_B<K, 1, T><<<grid, C::THREADS, sm, v.st>>>(dst, p, cB, v.ainv, v.mesh);
-  else k_B<K, 2, T><<<grid, C::THREADS, sm, v.st>>>(dst, p, cB, v.ainv, v.mesh);
-  ATM_CHECK_LAUNCH("k_B");
-  return ATM_OK;
-}
-
-template <int K, typename T>
-int CD_launch(const OpView<T> &v, T *dst, const T *w, const T *p, const T *pfix, T cC,
-              int mode) {
-  using C = Cfg<K>;
-  const int grid = (v.nc + C::CPB - 1) / C::CPB;
-  const size_t sm = smem_bytes<K, T>(4, 1);
-  switch (mode) {
-    case 0: k_CD<K, 0, T><<<grid, C::THREADS, sm, v.st>>>(dst, w, p, pfix, cC, v.invd, v.mesh); break;
-    case 1: k_CD<K, 1, T><<<grid, C::THREADS, sm, v.st>>>(dst, w, p, pfix, cC, v.invd, v.mesh); break;
-    case 2: k_CD<K, 2, T><<<grid, C::THREADS, sm, v.st>>>(dst, w, p, pfix, cC, v.invd, v.mesh); break;
-    default: k_CD<K, 3, T><<<grid, C::THREADS, sm, v.st>>>(dst, w, p, pfix, cC, v.invd, v.mesh); break;
-  }
-  ATM_CHECK_LAUNCH("k_CD");
-  return ATM_OK;
-}
-
 template <int K, typename T>
 int mass_launch(const OpView<T> &v, T *dst, const T *src, int ncomp, const T *weight,
                 T scale) {
@@ -507,18 +275,6 @@ int block_apply_launch(const OpView<T> &v, T *dst, const T *src, const T *binv, 
   return ATM_OK;
 }
 }  // namespace
-
-#define ATM_DISPATCH_K(kk, call)          \
-  switch (kk) {                           \
-    case 1: { constexpr int K = 1; return call; } \
-    case 2: { constexpr int K = 2; return call; } \
-    case 3: { constexpr int K = 3; return call; } \
-    case 4: { constexpr int K = 4; return call; } \
-    case 5: { constexpr int K = 5; return call; } \
-    default: return ATM_BAD_ARG;          \
-  }
-
-// ---- FP64 operator launchers (timed) -------------------------------------
 int launch_B(const atm_ctx &c, double *dst, const double *p, double coeff, int mode) {
   const double ns = (double)c.nc * c.nn2;
   // p read; B p written (2 comps); mode 1 reads dst too; mode 2 reads A^{-1}
@@ -528,7 +284,8 @@ int launch_B(const atm_ctx &c, double *dst, const double *p, double coeff, int m
                                4.0 * (2 * fl_face(c.k) + 2 * fl_face(c.k)) +
                                (mode == 2 ? 4.0 * c.nn2 * c.nn2 : 0.0));
   TimedRegion tr(c, KF_B, bytes, flops);
-  ATM_DISPATCH_K(c.k, (B_launch<K, double>(view(c), dst, p, coeff, mode)));
+  if (c.mesh.nhang > 0) return launch_B_hang(c, dst, p, coeff, mode);
+  ATM_DISPATCH_K(c.k, (B_launch<K, double, false>(schur_view(c), dst, p, coeff, mode)));
 }
 int launch_CD(const atm_ctx &c, double *dst, const double *w, const double *p,
               const double *pfix, double coeff, int mode) {
@@ -539,7 +296,8 @@ int launch_CD(const atm_ctx &c, double *dst, const double *w, const double *p,
   const double flops = c.nc * ((wd ? 4 : 3) * fl_eval(c.k) + fl_integrate(c.k, true) +
                                4.0 * (2 * 3 * fl_face(c.k) + fl_face(c.k)));
   TimedRegion tr(c, KF_CD, bytes, flops);
-  ATM_DISPATCH_K(c.k, (CD_launch<K, double>(view(c), dst, w, p, pfix, coeff, mode)));
+  if (c.mesh.nhang > 0) return launch_CD_hang(c, dst, w, p, pfix, coeff, mode);
+  ATM_DISPATCH_K(c.k, (CD_launch<K, double, false>(schur_view(c), dst, w, p, pfix, coeff, mode)));
 }
 int launch_mass(const atm_ctx &c, double *dst, const double *src, int ncomp,
                 const double *weight, double scale) {
@@ -548,12 +306,12 @@ int launch_mass(const atm_ctx &c, double *dst, const double *src, int ncomp,
   const double flops = c.nc * ((ncomp + (weight ? 1 : 0)) * fl_eval(c.k) +
                                ncomp * fl_integrate(c.k, false));
   TimedRegion tr(c, KF_MASS, bytes, flops);
-  ATM_DISPATCH_K(c.k, (mass_launch<K, double>(view(c), dst, src, ncomp, weight, scale)));
+  ATM_DISPATCH_K(c.k, (mass_launch<K, double>(schur_view(c), dst, src, ncomp, weight, scale)));
 }
 int launch_inv_diag(const atm_ctx &c, double *out, int ncomp, const double *weight,
                     double scale) {
   TimedRegion tr(c, KF_DIAG, 8.0 * c.nc * c.nn2 * (ncomp + (weight ? 1 : 0)), 0.0);
-  ATM_DISPATCH_K(c.k, (invdiag_launch<K, double>(view(c), out, ncomp, weight, scale)));
+  ATM_DISPATCH_K(c.k, (invdiag_launch<K, double>(schur_view(c), out, ncomp, weight, scale)));
 }
 int launch_block_inverse(const atm_ctx &c, double *out, const double *weight) {
   const double nn = c.nn, nq = c.nq, nn2 = c.nn2;
@@ -561,7 +319,7 @@ int launch_block_inverse(const atm_ctx &c, double *out, const double *weight) {
   const double bytes = 8.0 * c.nc * (nn2 * (weight ? 1 : 0) + nn2 * nn2);
   const double flops = c.nc * (2.0 * (nq * nn * nn * nq + nn2 * nn2 * nq) + 2.0 * nn2 * nn2 * nn2);
   TimedRegion tr(c, KF_BLOCK_INV, bytes, flops);
-  ATM_DISPATCH_K(c.k, (block_inverse_launch<K, double>(view(c), out, weight)));
+  ATM_DISPATCH_K(c.k, (block_inverse_launch<K, double>(schur_view(c), out, weight)));
 }
 int launch_block_apply(const atm_ctx &c, double *dst, const double *src, const double *binv,
                        int ncomp, double scale) {
@@ -569,20 +327,20 @@ int launch_block_apply(const atm_ctx &c, double *dst, const double *src, const d
   const double bytes = 8.0 * c.nc * (nn2 * nn2 + 2.0 * ncomp * nn2);
   const double flops = 2.0 * c.nc * ncomp * nn2 * nn2;
   TimedRegion tr(c, KF_BLOCK_APPLY, bytes, flops);
-  ATM_DISPATCH_K(c.k, (block_apply_launch<K, double>(view(c), dst, src, binv, ncomp, scale)));
+  ATM_DISPATCH_K(c.k, (block_apply_launch<K, double>(schur_view(c), dst, src, binv, ncomp, scale)));
 }
 
 // ---- launchers on a multigrid level (untimed; float or double) -----------
 template <typename T>
 int level_B(const LevelViewT<T> &v, T *dst, const T *p, T cB, int mode) {
   OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st};
-  ATM_DISPATCH_K(v.k, (B_launch<K, T>(o, dst, p, cB, mode)));
+  ATM_DISPATCH_K(v.k, (B_launch<K, T, false>(o, dst, p, cB, mode)));
 }
 template <typename T>
 int level_CD(const LevelViewT<T> &v, T *dst, const T *w, const T *p, const T *pfix, T cC,
              int mode) {
   OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st};
-  ATM_DISPATCH_K(v.k, (CD_launch<K, T>(o, dst, w, p, pfix, cC, mode)));
+  ATM_DISPATCH_K(v.k, (CD_launch<K, T, false>(o, dst, w, p, pfix, cC, mode)));
 }
 template <typename T>
 int level_inv_diag(const LevelViewT<T> &v, T *out, T scale) {

@@ -538,6 +538,11 @@ int mg_add_level(atm_ctx &c, int n_cells, int mapdeg, const double *nodes, int n
     set_error("atm_mg_add_level: need n_cells >= 1 and a children table");
     return ATM_BAD_ARG;
   }
+  if (c.mesh.nhang > 0) {
+    set_error("atm_mg_add_level: the multigrid hierarchy needs a conforming mesh "
+              "(this mesh has hanging faces)");
+    return ATM_BAD_ARG;
+  }
   if (!c.mg) {
     MG *mg = new MG();
     HostMesh hm;
@@ -580,6 +585,10 @@ int mg_add_level(atm_ctx &c, int n_cells, int mapdeg, const double *nodes, int n
   HostMesh hm;
   int rc = build_mesh_tables(c.k, n_cells, mapdeg, nodes, n_inner, inner, n_bdry, bdry, hm);
   if (rc) return rc;
+  if (hm.nhang > 0) {
+    set_error("atm_mg_add_level: coarse levels must be conforming meshes");
+    return ATM_BAD_ARG;
+  }
   mg.hm.push_back(std::move(hm));
   mg.ncells.push_back(n_cells);
   mg.children.push_back(std::move(ch));

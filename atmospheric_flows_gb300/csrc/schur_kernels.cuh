@@ -1,0 +1,263 @@
+// Schur-complement kernels shared by the conforming and the hanging-face
+// builds: B (pressure gradient, then optionally the exact cell-wise A^{-1})
+// and C/D (enthalpy divergence, internal-energy mass, Jacobi scale).
+//   B   euler_operator.h:1512-1617
+//   C   euler_operator.h:1413-1507
+//   D   euler_operator.h:1386-1408
+// HG selects the face loop with hanging faces (2:1 adaptive meshes).
+// Included by impl_kernels.cu (HG = false) and hang_kernels.cu (HG = true).
+#pragma once
+#include "atm_device.cuh"
+
+namespace atm {
+
+// ====================================================================== B ===
+// MODE 0: dst = B p ; 1: dst -= B p ; 2: dst = A^{-1} B p
+template <int K, int MODE, typename T, bool HG>
+__global__ void __launch_bounds__(Cfg<K>::THREADS)
+    k_B(T *__restrict__ dst, const T *__restrict__ p, T cB,
+        const T *__restrict__ ainv, MeshT<T> mesh) {
+  using C = Cfg<K>;
+  constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2, CPB = C::CPB;
+  constexpr int NT = 1;
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  T *sm = reinterpret_cast<T *>(sm_raw);
+  T *tiles = sm;
+  T *xab = tiles + CPB * NT * NN2;  // [CPB][2][2][NN*NQ]
+  T *fb = xab + CPB * 4 * NN * NQ;  // [CPB][2][4][NQ]
+  T *bt = fb + CPB * 8 * NQ;        // [CPB][2][NN2] (MODE 2)
+  T *fh = bt + CPB * 2 * NN2;       // [CPB][2][4][NQ] subface-1 values (HG)
+  const int tid = threadIdx.x, lc = tid / NQ, col = tid - lc * NQ;
+  const int c0 = blockIdx.x * CPB;
+  const int cnt = min(CPB, mesh.nc - c0);
+  load_tiles<K>(tiles, NT, 0, p, 1, c0, cnt);
+  __syncthreads();
+  const bool active = lc < cnt;
+  const int c = c0 + lc;
+  T Sx[NN], Dx[NN];
+  load_rows<K>(col, Sx, Dx);
+  if (active) {
+    const T *tl = tiles + lc * NT * NN2;
+    T pv[NQ];
+    eval_col<K>(tl, Sx, pv);
+    const T *G = mesh.qgeo + (long)c * 5 * NQ2;
+    T V[NQ], Gxi[NQ], Get[NQ];
+    // submit_divergence(-cB p): component d is tested with d(phi)/dx_d
+#pragma unroll
+    for (int comp = 0; comp < 2; ++comp) {
+#pragma unroll
+      for (int qz = 0; qz < NQ; ++qz) {
+        const auto g = qgeo<K>(G, qz * NQ + col);
+        const T s = -cB * pv[qz];
+        Gxi[qz] = (comp == 0 ? g.xx : g.xz) * s;
+        Get[qz] = (comp == 0 ? g.ex : g.ez) * s;
+        V[qz] = T(0.0);
+      }
+      T *xa = xab + (lc * 2 + comp) * 2 * NN * NQ;
+      integrate_col_z<K, false, true>(V, Gxi, Get, xa, xa + NN * NQ, col);
+    }
+    face_terms<K, 2, HG>(mesh, c, col, Sx, fb + lc * 2 * 4 * NQ, fh + lc * 2 * 4 * NQ,
+                         [&](int f, int nb, int nf, T n0, T n1, T jxw, const auto &Ro,
+                             const auto &Rn, auto &val) {
+      const T pp = face_val<K>(tl, f, Ro);
+      T avg;
+      if (nb >= 0) {
+        const T pm = face_val<K>(p + (long)nb * NN2, nf, Rn);
+        avg = T(0.5) * (pp + pm);
+      } else {
+        avg = T(0.5) * (pp + pp);  // wall, p_D = p
+      }
+      val[0] = cB * avg * n0 * jxw;
+      val[1] = cB * avg * n1 * jxw;
+    });
+  }
+  __syncthreads();
+  if (active && col < NN) {
+    T St[NQ], Dt[NQ];
+    load_cols<K>(col, St, Dt);
+#pragma unroll
+    for (int comp = 0; comp < 2; ++comp) {
+      T out[NN];
+      const T *xa = xab + (lc * 2 + comp) * 2 * NN * NQ;
+      integrate_out<K, true>(xa, xa + NN * NQ, St, Dt, out);
+      add_faces<K, HG>(mesh, c, fb + (lc * 2 + comp) * 4 * NQ, fh + (lc * 2 + comp) * 4 * NQ,
+                       col, St, out);
+      if (MODE == 2) {
+#pragma unroll
+        for (int iz = 0; iz < NN; ++iz) bt[(lc * 2 + comp) * NN2 + iz * NN + col] = out[iz];
+      } else {
+        T *d = dst + ((long)c * 2 + comp) * NN2;
+#pragma unroll
+        for (int iz = 0; iz < NN; ++iz) {
+          if (MODE == 0) d[iz * NN + col] = out[iz];
+          else d[iz * NN + col] -= out[iz];
+        }
+      }
+    }
+  }
+  if (MODE == 2) {
+    __syncthreads();
+    if (active) {
+      const T *Ab = ainv + (long)c * NN2 * NN2;
+      const T *b0 = bt + (lc * 2 + 0) * NN2, *b1 = bt + (lc * 2 + 1) * NN2;
+      for (int i = col; i < NN2; i += NQ) {
+        T s0 = T(0.0), s1 = T(0.0);
+#pragma unroll 5
+        for (int j = 0; j < NN2; ++j) {
+          const T a = Ab[j * NN2 + i];  // transposed storage
+          s0 = fma(a, b0[j], s0);
+          s1 = fma(a, b1[j], s1);
+        }
+        dst[((long)c * 2 + 0) * NN2 + i] = s0;
+        dst[((long)c * 2 + 1) * NN2 + i] = s1;
+      }
+    }
+  }
+}
+
+// ===================================================================== CD ===
+// MODE 0: dst = C w ; 1: dst = sD D p - C w ; 2: dst = invd .* (sD D p - C w)
+// MODE 3: dst -= C w
+template <int K, int MODE, typename T, bool HG>
+__global__ void __launch_bounds__(Cfg<K>::THREADS)
+    k_CD(T *__restrict__ dst, const T *__restrict__ w, const T *__restrict__ p,
+         const T *__restrict__ pfix, T cC, const T *__restrict__ invd,
+         MeshT<T> mesh) {
+  using C = Cfg<K>;
+  constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2, CPB = C::CPB;
+  constexpr bool WITH_D = (MODE == 1 || MODE == 2);
+  constexpr int NT = WITH_D ? 4 : 3;  // w(2), pfix, [p]
+  constexpr T GM1 = GAS_GAMMA - T(1.0);
+  constexpr T HG_ = GAS_GAMMA / (GAS_GAMMA - T(1.0));  // enthalpy factor
+  // sign of the C contribution in dst
+  constexpr T SC = WITH_D ? -T(1.0) : T(1.0);
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  T *sm = reinterpret_cast<T *>(sm_raw);
+  T *tiles = sm;
+  T *xab = tiles + CPB * NT * NN2;
+  T *fb = xab + CPB * 2 * NN * NQ;
+  T *fh = fb + CPB * 4 * NQ;  // subface-1 values (HG)
+  const int tid = threadIdx.x, lc = tid / NQ, col = tid - lc * NQ;
+  const int c0 = blockIdx.x * CPB;
+  const int cnt = min(CPB, mesh.nc - c0);
+  load_tiles<K>(tiles, NT, 0, w, 2, c0, cnt);
+  load_tiles<K>(tiles, NT, 2, pfix, 1, c0, cnt);
+  if (WITH_D) load_tiles<K>(tiles, NT, 3, p, 1, c0, cnt);
+  __syncthreads();
+  const bool active = lc < cnt;
+  const int c = c0 + lc;
+  T Sx[NN], Dx[NN];
+  load_rows<K>(col, Sx, Dx);
+  if (active) {
+    const T *tl = tiles + lc * NT * NN2;
+    T wx[NQ], wz[NQ], pf[NQ], pv[NQ];
+    eval_col<K>(tl, Sx, wx);
+    eval_col<K>(tl + NN2, Sx, wz);
+    eval_col<K>(tl + 2 * NN2, Sx, pf);
+    if (WITH_D) eval_col<K>(tl + 3 * NN2, Sx, pv);
+    const T *G = mesh.qgeo + (long)c * 5 * NQ2;
+    T V[NQ], Gxi[NQ], Get[NQ];
+#pragma unroll
+    for (int qz = 0; qz < NQ; ++qz) {
+      const auto g = qgeo<K>(G, qz * NQ + col);
+      // C: submit_gradient(-cC hg pfix w)
+      const T gx = SC * (-cC * HG_ * pf[qz] * wx[qz]);
+      const T gz = SC * (-cC * HG_ * pf[qz] * wz[qz]);
+      Gxi[qz] = g.xx * gx + g.xz * gz;
+      Get[qz] = g.ex * gx + g.ez * gz;
+      V[qz] = WITH_D ? (T(1.0) / GM1) * pv[qz] * g.jxw : T(0.0);
+    }
+    T *xa = xab + lc * 2 * NN * NQ;
+    integrate_col_z<K, WITH_D, true>(V, Gxi, Get, xa, xa + NN * NQ, col);
+    face_terms<K, 1, HG>(mesh, c, col, Sx, fb + lc * 4 * NQ, fh + lc * 4 * NQ,
+                         [&](int f, int nb, int nf, T n0, T n1, T jxw, const auto &Ro,
+                             const auto &Rn, auto &val) {
+      if (nb < 0) {
+        val[0] = T(0.0);
+        return;
+      }
+      const T wxp = face_val<K>(tl, f, Ro), wzp = face_val<K>(tl + NN2, f, Ro);
+      const T pfp = face_val<K>(tl + 2 * NN2, f, Ro);
+      const T wxm = face_val<K>(w + (long)nb * 2 * NN2, nf, Rn);
+      const T wzm = face_val<K>(w + ((long)nb * 2 + 1) * NN2, nf, Rn);
+      const T pfm = face_val<K>(pfix + (long)nb * NN2, nf, Rn);
+      const T av0 = T(0.5) * HG_ * (pfp * wxp + pfm * wxm);
+      const T av1 = T(0.5) * HG_ * (pfp * wzp + pfm * wzm);
+      const T lam = fmax(fabs(wxp * n0 + wzp * n1), fabs(wxm * n0 + wzm * n1));
+      const T je = T(1.0) / GM1 * (pfp - pfm);
+      val[0] = SC * cC * ((av0 * n0 + av1 * n1) + T(0.5) * lam * je) * jxw;
+    });
+  }
+  __syncthreads();
+  if (active && col < NN) {
+    T St[NQ], Dt[NQ], out[NN];
+    load_cols<K>(col, St, Dt);
+    const T *xa = xab + lc * 2 * NN * NQ;
+    integrate_out<K, true>(xa, xa + NN * NQ, St, Dt, out);
+    add_faces<K, HG>(mesh, c, fb + lc * 4 * NQ, fh + lc * 4 * NQ, col, St, out);
+    T *d = dst + (long)c * NN2;
+#pragma unroll
+    for (int iz = 0; iz < NN; ++iz) {
+      const int i = iz * NN + col;
+      if (MODE == 2) d[i] = invd[(long)c * NN2 + i] * out[iz];
+      else if (MODE == 3) d[i] -= out[iz];
+      else d[i] = out[iz];
+    }
+  }
+}
+
+// ============================================================ launchers ===
+template <typename T>
+struct OpView {
+  int k, nc;
+  MeshT<T> mesh;
+  const T *ainv;
+  const T *invd;
+  cudaStream_t st;
+};
+
+inline OpView<double> schur_view(const atm_ctx &c) {
+  return OpView<double>{c.k, c.nc, c.mesh, c.ainv, c.invdiag_D, c.stream};
+}
+
+template <int K, typename T, bool HG>
+int B_launch(const OpView<T> &v, T *dst, const T *p, T cB, int mode) {
+  using C = Cfg<K>;
+  const int grid = (v.nc + C::CPB - 1) / C::CPB;
+  const size_t sm = smem_bytes<K, T>(1, 2, HG) + sizeof(T) * C::CPB * 2 * C::NN2;
+  if (mode == 0) k_B<K, 0, T, HG><<<grid, C::THREADS, sm, v.st>>>(dst, p, cB, v.ainv, v.mesh);
+  else if (mode == 1) k_B<K, 1, T, HG><<<grid, C::THREADS, sm, v.st>>>(dst, p, cB, v.ainv, v.mesh);
+  else k_B<K, 2, T, HG><<<grid, C::THREADS, sm, v.st>>>(dst, p, cB, v.ainv, v.mesh);
+  ATM_CHECK_LAUNCH("k_B");
+  return ATM_OK;
+}
+
+template <int K, typename T, bool HG>
+int CD_launch(const OpView<T> &v, T *dst, const T *w, const T *p, const T *pfix, T cC,
+              int mode) {
+  using C = Cfg<K>;
+  const int grid = (v.nc + C::CPB - 1) / C::CPB;
+  const size_t sm = smem_bytes<K, T>(4, 1, HG);
+  switch (mode) {
+    case 0: k_CD<K, 0, T, HG><<<grid, C::THREADS, sm, v.st>>>(dst, w, p, pfix, cC, v.invd, v.mesh); break;
+    case 1: k_CD<K, 1, T, HG><<<grid, C::THREADS, sm, v.st>>>(dst, w, p, pfix, cC, v.invd, v.mesh); break;
+    case 2: k_CD<K, 2, T, HG><<<grid, C::THREADS, sm, v.st>>>(dst, w, p, pfix, cC, v.invd, v.mesh); break;
+    default: k_CD<K, 3, T, HG><<<grid, C::THREADS, sm, v.st>>>(dst, w, p, pfix, cC, v.invd, v.mesh); break;
+  }
+  ATM_CHECK_LAUNCH("k_CD");
+  return ATM_OK;
+}
+
+
+#define ATM_DISPATCH_K(kk, call)          \
+  switch (kk) {                           \
+    case 1: { constexpr int K = 1; return call; } \
+    case 2: { constexpr int K = 2; return call; } \
+    case 3: { constexpr int K = 3; return call; } \
+    case 4: { constexpr int K = 4; return call; } \
+    case 5: { constexpr int K = 5; return call; } \
+    default: return ATM_BAD_ARG;          \
+  }
+
+
+}  // namespace atm

@@ -18,6 +18,7 @@ namespace atm {
 
 int upload_basis_rhs(const double *t);
 int upload_basis_impl(const double *t);
+int upload_basis_hang(const double *t);
 
 // Legendre P_n(x) and P_n'(x) by the three-term recurrence
 static void legendre_pd(int n, double x, double *p, double *dp) {
@@ -108,15 +109,24 @@ int upload_basis_all() {
   ATM_CUDA(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> lock(mu);
   if (dev >= 0 && dev < 64 && done[dev]) return ATM_OK;
-  std::vector<double> tab((KMAX + 1) * 2 * NQ_MAX * NN_MAX, 0.0);
+  // [k][w][q*(k+1)+i]: w = 0 values, 1 derivatives at the Gauss points,
+  // 2 and 3 values at the subface points (g_q + s)/2 (hanging faces)
+  constexpr int NW = 4;
+  std::vector<double> tab((KMAX + 1) * NW * NQ_MAX * NN_MAX, 0.0);
   for (int k = 1; k <= KMAX; ++k) {
     HostBasis b = make_basis(k);
-    double *S = &tab[(k * 2 + 0) * NQ_MAX * NN_MAX];
-    double *D = &tab[(k * 2 + 1) * NQ_MAX * NN_MAX];
+    double *S = &tab[(k * NW + 0) * NQ_MAX * NN_MAX];
+    double *D = &tab[(k * NW + 1) * NQ_MAX * NN_MAX];
     std::memcpy(S, b.S.data(), b.S.size() * sizeof(double));
     std::memcpy(D, b.D.data(), b.D.size() * sizeof(double));
+    for (int s = 0; s < 2; ++s) {
+      double *H = &tab[(k * NW + 2 + s) * NQ_MAX * NN_MAX];
+      for (int q = 0; q < b.nq; ++q)
+        lagrange_eval(b.gll, 0.5 * (b.gauss[q] + s), &H[q * b.nn], nullptr);
+    }
   }
-  if (upload_basis_rhs(tab.data()) || upload_basis_impl(tab.data())) {
+  if (upload_basis_rhs(tab.data()) || upload_basis_impl(tab.data()) ||
+      upload_basis_hang(tab.data())) {
     set_error("failed to upload basis tables to constant memory");
     return ATM_CUDA_ERROR;
   }
@@ -130,8 +140,11 @@ void mesh_free(Mesh &m) {
   cudaFree(m.nbr);
   cudaFree(m.nbrf);
   cudaFree(m.minv);
-  m.qgeo = m.fgeo = m.minv = nullptr;
-  m.nbr = m.nbrf = nullptr;
+  cudaFree(m.hnb);
+  cudaFree(m.hgeo);
+  m.qgeo = m.fgeo = m.minv = m.hgeo = nullptr;
+  m.nbr = m.nbrf = m.hnb = nullptr;
+  m.nhang = 0;
 }
 
 int build_mesh_tables(int k, int nc, int mapdeg, const double *nodes, int n_inner,
@@ -141,10 +154,15 @@ int build_mesh_tables(int k, int nc, int mapdeg, const double *nodes, int n_inne
     set_error("mesh tables: bad mapping degree or null table");
     return ATM_BAD_ARG;
   }
-  // --- connectivity
+  // --- connectivity.  inner face: (c+, f+, c-, f-, o); o = 0 conforming,
+  // o = 1, 2: c+ is the fine cell and its face f+ is subface o-1 of face f-
+  // of the coarse cell c- (2:1 adaptive meshes, deal.II puts the fine cell
+  // on the interior side of a hanging face).
   std::vector<int> &nbr = out.nbr, &nbrf = out.nbrf;
   nbr.assign((size_t)nc * 4, -2);
   nbrf.assign((size_t)nc * 4, -1);
+  std::vector<int> hidx((size_t)nc * 4, -1);
+  out.hnb.clear();
   for (int f = 0; f < n_inner; ++f) {
     const int *e = inner + 5L * f;
     if (e[0] < 0 || e[0] >= nc || e[2] < 0 || e[2] >= nc || e[1] < 0 || e[1] > 3 ||
@@ -152,18 +170,57 @@ int build_mesh_tables(int k, int nc, int mapdeg, const double *nodes, int n_inne
       set_error("inner face " + std::to_string(f) + ": cell or face index out of range");
       return ATM_BAD_ARG;
     }
-    if (e[4] != 0) {
-      set_error("inner face " + std::to_string(f) + ": only orientation 0 is supported");
+    if (e[4] < 0 || e[4] > 2) {
+      set_error("inner face " + std::to_string(f) +
+                ": the last entry must be 0 (conforming) or 1, 2 (hanging subface)");
+      return ATM_BAD_ARG;
+    }
+    if ((e[1] >> 1) != (e[3] >> 1) || e[1] == e[3]) {
+      set_error("inner face " + std::to_string(f) +
+                ": the two sides must be opposite faces (0/1 or 2/3)");
       return ATM_BAD_ARG;
     }
     const size_t a = (size_t)e[0] * 4 + e[1], b = (size_t)e[2] * 4 + e[3];
-    if (nbr[a] != -2 || nbr[b] != -2) {
+    if (nbr[a] != -2) {
       set_error("inner face " + std::to_string(f) + ": cell face listed twice");
       return ATM_BAD_ARG;
     }
-    nbr[a] = e[2]; nbrf[a] = e[3];
-    nbr[b] = e[0]; nbrf[b] = e[1];
+    nbr[a] = e[2];
+    nbrf[a] = e[3] | (e[4] << 2);
+    if (e[4] == 0) {
+      if (nbr[b] != -2) {
+        set_error("inner face " + std::to_string(f) + ": cell face listed twice");
+        return ATM_BAD_ARG;
+      }
+      nbr[b] = e[0];
+      nbrf[b] = e[1];
+    } else {
+      if (hidx[b] < 0) {
+        if (nbr[b] != -2) {
+          set_error("inner face " + std::to_string(f) +
+                    ": coarse face is also listed as a conforming or boundary face");
+          return ATM_BAD_ARG;
+        }
+        hidx[b] = (int)(out.hnb.size() / 2);
+        out.hnb.push_back(-1);
+        out.hnb.push_back(-1);
+        nbr[b] = hidx[b];
+        nbrf[b] = e[1] | (3 << 2);
+      }
+      int &slot = out.hnb[(size_t)hidx[b] * 2 + (e[4] - 1)];
+      if (slot != -1) {
+        set_error("inner face " + std::to_string(f) + ": hanging subface listed twice");
+        return ATM_BAD_ARG;
+      }
+      slot = e[0];
+    }
   }
+  out.nhang = (int)(out.hnb.size() / 2);
+  for (int h = 0; h < out.nhang; ++h)
+    if (out.hnb[2 * h] < 0 || out.hnb[2 * h + 1] < 0) {
+      set_error("hanging face " + std::to_string(h) + ": only one of its two subfaces is listed");
+      return ATM_BAD_ARG;
+    }
   for (int f = 0; f < n_bdry; ++f) {
     const int *e = bdry + 3L * f;
     if (e[0] < 0 || e[0] >= nc || e[1] < 0 || e[1] > 3) {
@@ -171,7 +228,7 @@ int build_mesh_tables(int k, int nc, int mapdeg, const double *nodes, int n_inne
       return ATM_BAD_ARG;
     }
     const size_t a = (size_t)e[0] * 4 + e[1];
-    if (nbr[a] != -2) {
+    if (nbr[a] != -2 || hidx[a] >= 0) {
       set_error("boundary face " + std::to_string(f) + ": cell face listed twice");
       return ATM_BAD_ARG;
     }
@@ -213,6 +270,29 @@ int build_mesh_tables(int k, int nc, int mapdeg, const double *nodes, int n_inne
         }
       }
   };
+  // outward unit normal and face weight of face f at the face parameter
+  // whose mapping-basis values are (Lt, dLt); written to o[0], o[st], o[2 st]
+  auto face_geo = [&](int cell, int f, const double *Lt, const double *dLt, double w,
+                      double *o, int st) {
+    const double *La, *dLa, *Lb, *dLb;
+    double nr0, nr1;
+    switch (f) {
+      case 0: La = L0.data(); dLa = dL0.data(); Lb = Lt; dLb = dLt; nr0 = -1; nr1 = 0; break;
+      case 1: La = L1.data(); dLa = dL1.data(); Lb = Lt; dLb = dLt; nr0 = 1; nr1 = 0; break;
+      case 2: La = Lt; dLa = dLt; Lb = L0.data(); dLb = dL0.data(); nr0 = 0; nr1 = -1; break;
+      default: La = Lt; dLa = dLt; Lb = L1.data(); dLb = dL1.data(); nr0 = 0; nr1 = 1; break;
+    }
+    double J[4];
+    jac(cell, La, dLa, Lb, dLb, J);
+    const double det = J[0] * J[3] - J[1] * J[2];
+    // physical normal ~ J^{-T} n_ref; |J^{-T} n_ref| det = face metric
+    const double t0 = (J[3] * nr0 - J[2] * nr1) / det;
+    const double t1 = (-J[1] * nr0 + J[0] * nr1) / det;
+    const double len = std::sqrt(t0 * t0 + t1 * t1);
+    o[0] = t0 / len;
+    o[st] = t1 / len;
+    o[2 * st] = det * len * w;
+  };
   for (int cell = 0; cell < nc; ++cell) {
     for (int qz = 0; qz < nq; ++qz)
       for (int qx = 0; qx < nq; ++qx) {
@@ -233,25 +313,22 @@ int build_mesh_tables(int k, int nc, int mapdeg, const double *nodes, int n_inne
       }
     for (int f = 0; f < 4; ++f)
       for (int q = 0; q < nq; ++q) {
-        const double *La, *dLa, *Lb, *dLb;
-        double nr0, nr1;
-        switch (f) {
-          case 0: La = L0.data(); dLa = dL0.data(); Lb = Lg[q].data(); dLb = dLg[q].data(); nr0 = -1; nr1 = 0; break;
-          case 1: La = L1.data(); dLa = dL1.data(); Lb = Lg[q].data(); dLb = dLg[q].data(); nr0 = 1; nr1 = 0; break;
-          case 2: La = Lg[q].data(); dLa = dLg[q].data(); Lb = L0.data(); dLb = dL0.data(); nr0 = 0; nr1 = -1; break;
-          default: La = Lg[q].data(); dLa = dLg[q].data(); Lb = L1.data(); dLb = dL1.data(); nr0 = 0; nr1 = 1; break;
-        }
-        double J[4];
-        jac(cell, La, dLa, Lb, dLb, J);
-        const double det = J[0] * J[3] - J[1] * J[2];
-        // physical normal ~ J^{-T} n_ref; |J^{-T} n_ref| det = face metric
-        const double t0 = (J[3] * nr0 - J[2] * nr1) / det;
-        const double t1 = (-J[1] * nr0 + J[0] * nr1) / det;
-        const double len = std::sqrt(t0 * t0 + t1 * t1);
         const size_t base = ((size_t)cell * 4 + f) * 3 * nq;
-        fgeo[base + q] = t0 / len;
-        fgeo[base + nq + q] = t1 / len;
-        fgeo[base + 2 * nq + q] = det * len * b.weights[q];
+        face_geo(cell, f, Lg[q].data(), dLg[q].data(), b.weights[q], &fgeo[base + q], nq);
+      }
+  }
+  // subface geometry of the coarse side of every hanging face, at the points
+  // (g_q + s)/2 of the coarse face with weights w_q/2
+  out.hgeo.assign((size_t)out.nhang * 2 * 3 * nq, 0.0);
+  std::vector<double> Ls, dLs;
+  for (size_t a = 0; a < hidx.size(); ++a) {
+    if (hidx[a] < 0) continue;
+    const int cell = (int)(a / 4), f = (int)(a % 4), h = hidx[a];
+    for (int s = 0; s < 2; ++s)
+      for (int q = 0; q < nq; ++q) {
+        tab(0.5 * (b.gauss[q] + s), Ls, dLs);
+        face_geo(cell, f, Ls.data(), dLs.data(), 0.5 * b.weights[q],
+                 &out.hgeo[((size_t)h * 2 + s) * 3 * nq + q], nq);
       }
   }
   return ATM_OK;
@@ -275,6 +352,13 @@ int mesh_upload(atm_ctx &c, int mapdeg, const double *nodes, int n_inner, const 
   ATM_CUDA(cudaMemcpyAsync(m.fgeo, hm.fgeo.data(), hm.fgeo.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
   ATM_CUDA(cudaMemcpyAsync(m.nbr, hm.nbr.data(), hm.nbr.size() * sizeof(int), cudaMemcpyHostToDevice, c.stream));
   ATM_CUDA(cudaMemcpyAsync(m.nbrf, hm.nbrf.data(), hm.nbrf.size() * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+  if (hm.nhang > 0) {
+    ATM_CUDA(cudaMalloc(&m.hnb, hm.hnb.size() * sizeof(int)));
+    ATM_CUDA(cudaMalloc(&m.hgeo, hm.hgeo.size() * sizeof(double)));
+    ATM_CUDA(cudaMemcpyAsync(m.hnb, hm.hnb.data(), hm.hnb.size() * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    ATM_CUDA(cudaMemcpyAsync(m.hgeo, hm.hgeo.data(), hm.hgeo.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+  }
+  m.nhang = hm.nhang;
   c.mapdeg = mapdeg;
   rc = launch_block_inverse(c, m.minv, nullptr);
   if (rc) return rc;

@@ -52,8 +52,15 @@ const char *atm_version(void);
  *   (Atmospheric_Flow.cc:279-409) re-uploaded as plain tables.
  *   mapping_nodes : [n_cells][(m+1)^2][2] host, Gauss-Lobatto points of a
  *                   degree-m tensor Lagrange mapping (MappingQ(m)), x fastest
- *   inner_faces   : [n_inner][5] host: cell+, face+, cell-, face-, orientation
- *                   (local faces 0:x=0 1:x=1 2:z=0 3:z=1; orientation must be 0)
+ *   inner_faces   : [n_inner][5] host: cell+, face+, cell-, face-, o
+ *                   (local faces 0:x=0 1:x=1 2:z=0 3:z=1; face+ and face- opposite).
+ *                   o = 0: conforming face.  o = 1, 2: hanging face of a 2:1
+ *                   adaptive mesh -- cell+ is the fine cell and its face is
+ *                   subface o-1 (the half at the lower face parameter for o = 1)
+ *                   of face- of the coarse cell cell-; both subfaces must be
+ *                   listed.  As deal.II, the fine side is the interior side.
+ *                   Replaces the hanging-face handling of MatrixFree on
+ *                   p4est meshes (Atmospheric_Flow.cc:279-283).
  *   bdry_faces    : [n_bdry][3] host: cell, face, boundary id (all walls)
  * ------------------------------------------------------------------------- */
 int atm_ctx_create(int dim, int degree, int n_cells, int mapping_degree,

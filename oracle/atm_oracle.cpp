@@ -158,13 +158,20 @@ struct Oracle {
   int k = 1, nn = 2, nq = 3, nc = 0, m = 1, mn = 2;
   int nn2 = 4, nq2 = 9;
   Vec S, D, W;  // [q][i] values / derivatives of the node basis at Gauss pts
+  Vec Sh[2];    // [q][i] values at the subface points (g_q + s)/2, s = 0, 1
   Vec cJinv, cJxW, cX;  // per cell per qp: dxi_a/dx_b (4), JxW, (x,z)
-  std::vector<int> inner, bdry;  // [nf][5] (c+,f+,c-,f-,orient), [nb][3]
+  // [nf][5] (c+,f+,c-,f-,o), [nb][3].  o = 0 conforming; o = 1, 2: hanging
+  // face, c+ is the fine cell and its face is subface o-1 of face f- of the
+  // coarse cell c- (deal.II: the fine cell is the interior side, the normal
+  // and JxW come from it, and the coarse side is evaluated on the subface).
+  std::vector<int> inner, bdry;
   int nf = 0, nb = 0;
   Vec fN, fJxW;  // inner faces, from the "+" side: [nf][nq][2], [nf][nq]
   Vec bN, bJxW;  // boundary faces
-  // cell -> face contributions: 4 entries per cell (type, index, side)
-  std::vector<int> cface;  // [nc][4][3]; type -1 none, 0 inner, 1 boundary
+  // cell -> face contributions: 2 slots per cell face (a coarse hanging face
+  // collects both subfaces): (type, index, side), type -1 none, 0 inner,
+  // 1 boundary
+  std::vector<int> cface;  // [nc][4][2][3]
 
   // parameters and tableau (euler_operator.h:220-240)
   double Ma = 1, Fr = 1, dt = 1;
@@ -218,6 +225,11 @@ struct Oracle {
         S[q * nn + i] = lagrange(xn, i, gx[q]);
         D[q * nn + i] = lagrange_d(xn, i, gx[q]);
       }
+    for (int s = 0; s < 2; ++s) {
+      Sh[s].assign(nq * nn, 0.0);
+      for (int q = 0; q < nq; ++q)
+        for (int i = 0; i < nn; ++i) Sh[s][q * nn + i] = lagrange(xn, i, 0.5 * (gx[q] + s));
+    }
     // mapping derivative tables at the Gauss points and at 0, 1
     auto map_eval = [&](int c, double xi, double eta, double *x, double *J) {
       // J = [[dx/dxi, dx/deta],[dz/dxi, dz/deta]]
@@ -293,18 +305,22 @@ struct Oracle {
       for (int q = 0; q < nq; ++q)
         face_geom(bdry[3 * f], bdry[3 * f + 1], q, &bN[((long)f * nq + q) * 2],
                   &bJxW[(long)f * nq + q]);
-    cface.assign((long)nc * 4 * 3, -1);
+    cface.assign((long)nc * 8 * 3, -1);
+    auto slot = [&](int c, int lf) {
+      int *e = &cface[((long)c * 4 + lf) * 2 * 3];
+      return e[0] < 0 ? e : e + 3;
+    };
     for (int f = 0; f < nf; ++f) {
       const int cp = inner[5 * f], fp = inner[5 * f + 1];
       const int cm = inner[5 * f + 2], fm = inner[5 * f + 3];
-      int *e = &cface[((long)cp * 4 + fp) * 3];
+      int *e = slot(cp, fp);
       e[0] = 0; e[1] = f; e[2] = 0;
-      e = &cface[((long)cm * 4 + fm) * 3];
+      e = slot(cm, fm);
       e[0] = 0; e[1] = f; e[2] = 1;
     }
     for (int f = 0; f < nb; ++f) {
       const int c = bdry[3 * f], lf = bdry[3 * f + 1];
-      int *e = &cface[((long)c * 4 + lf) * 3];
+      int *e = slot(c, lf);
       e[0] = 1; e[1] = f; e[2] = 0;
     }
   }
@@ -370,18 +386,21 @@ struct Oracle {
       default: return k * nn + i;
     }
   }
-  void eval_face(const double *u, int f, double *v) const {
+  // trace at the face points; sub >= 0: at the points of subface `sub`
+  void eval_face(const double *u, int f, double *v, int sub = -1) const {
+    const double *T = sub < 0 ? S.data() : Sh[sub].data();
     for (int q = 0; q < nq; ++q) {
       double s = 0.0;
-      for (int i = 0; i < nn; ++i) s += S[q * nn + i] * u[face_node(f, i)];
+      for (int i = 0; i < nn; ++i) s += T[q * nn + i] * u[face_node(f, i)];
       v[q] = s;
     }
   }
   // face contribution buffer entry (nn values) from flux F[q] (JxW included)
-  void integrate_face(const double *F, double *out) const {
+  void integrate_face(const double *F, double *out, int sub = -1) const {
+    const double *T = sub < 0 ? S.data() : Sh[sub].data();
     for (int i = 0; i < nn; ++i) {
       double s = 0.0;
-      for (int q = 0; q < nq; ++q) s += S[q * nn + i] * F[q];
+      for (int q = 0; q < nq; ++q) s += T[q * nn + i] * F[q];
       out[i] = s;
     }
   }
@@ -396,8 +415,9 @@ struct Oracle {
   void gather_faces(double *dst, int ncomp) const {
 #pragma omp parallel for
     for (int c = 0; c < nc; ++c)
-      for (int lf = 0; lf < 4; ++lf) {
-        const int *e = &cface[((long)c * 4 + lf) * 3];
+      for (int sl = 0; sl < 8; ++sl) {
+        const int lf = sl >> 1;
+        const int *e = &cface[((long)c * 8 + sl) * 3];
         if (e[0] < 0) continue;
         for (int comp = 0; comp < ncomp; ++comp) {
           const double *src = e[0] == 0
@@ -450,14 +470,15 @@ struct Oracle {
     for (int f = 0; f < nf; ++f) {
       const int cp = inner[5 * f], fp = inner[5 * f + 1];
       const int cm = inner[5 * f + 2], fm = inner[5 * f + 3];
+      const int hs = inner[5 * f + 4] - 1;  // subface of the "-" side, -1 conforming
       double rp[3][16], rm[3][16], uxp[3][16], uxm[3][16], uzp[3][16], uzm[3][16];
       for (int j = 0; j < nst; ++j) {
         eval_face(tile(src[2 * j], cp, 1, 0), fp, rp[j]);
-        eval_face(tile(src[2 * j], cm, 1, 0), fm, rm[j]);
+        eval_face(tile(src[2 * j], cm, 1, 0), fm, rm[j], hs);
         eval_face(tile(src[2 * j + 1], cp, 2, 0), fp, uxp[j]);
-        eval_face(tile(src[2 * j + 1], cm, 2, 0), fm, uxm[j]);
+        eval_face(tile(src[2 * j + 1], cm, 2, 0), fm, uxm[j], hs);
         eval_face(tile(src[2 * j + 1], cp, 2, 1), fp, uzp[j]);
-        eval_face(tile(src[2 * j + 1], cm, 2, 1), fm, uzm[j]);
+        eval_face(tile(src[2 * j + 1], cm, 2, 1), fm, uzm[j], hs);
       }
       double Fp[16], Fm[16];
       for (int q = 0; q < nq; ++q) {
@@ -476,7 +497,7 @@ struct Oracle {
         Fm[q] = flux * jxw;
       }
       integrate_face(Fp, &fbuf[((long)f * 2 + 0) * nn]);
-      integrate_face(Fm, &fbuf[((long)f * 2 + 1) * nn]);
+      integrate_face(Fm, &fbuf[((long)f * 2 + 1) * nn], hs);
     }
     gather_faces(dst, 1);
   }
@@ -546,17 +567,18 @@ struct Oracle {
     for (int f = 0; f < nf; ++f) {
       const int cp = inner[5 * f], fp = inner[5 * f + 1];
       const int cm = inner[5 * f + 2], fm = inner[5 * f + 3];
+      const int hs = inner[5 * f + 4] - 1;  // subface of the "-" side, -1 conforming
       double rp[3][16], rm[3][16], uxp[3][16], uxm[3][16], uzp[3][16], uzm[3][16],
           pp_[3][16], pm[3][16];
       for (int j = 0; j < nst; ++j) {
         eval_face(tile(src[3 * j], cp, 1, 0), fp, rp[j]);
-        eval_face(tile(src[3 * j], cm, 1, 0), fm, rm[j]);
+        eval_face(tile(src[3 * j], cm, 1, 0), fm, rm[j], hs);
         eval_face(tile(src[3 * j + 1], cp, 2, 0), fp, uxp[j]);
-        eval_face(tile(src[3 * j + 1], cm, 2, 0), fm, uxm[j]);
+        eval_face(tile(src[3 * j + 1], cm, 2, 0), fm, uxm[j], hs);
         eval_face(tile(src[3 * j + 1], cp, 2, 1), fp, uzp[j]);
-        eval_face(tile(src[3 * j + 1], cm, 2, 1), fm, uzm[j]);
+        eval_face(tile(src[3 * j + 1], cm, 2, 1), fm, uzm[j], hs);
         eval_face(tile(src[3 * j + 2], cp, 1, 0), fp, pp_[j]);
-        eval_face(tile(src[3 * j + 2], cm, 1, 0), fm, pm[j]);
+        eval_face(tile(src[3 * j + 2], cm, 1, 0), fm, pm[j], hs);
       }
       double Fp0[16], Fp1[16], Fm0[16], Fm1[16];
       for (int q = 0; q < nq; ++q) {
@@ -581,8 +603,8 @@ struct Oracle {
       }
       integrate_face(Fp0, &fbuf[(((long)f * 2 + 0) * 2 + 0) * nn]);
       integrate_face(Fp1, &fbuf[(((long)f * 2 + 0) * 2 + 1) * nn]);
-      integrate_face(Fm0, &fbuf[(((long)f * 2 + 1) * 2 + 0) * nn]);
-      integrate_face(Fm1, &fbuf[(((long)f * 2 + 1) * 2 + 1) * nn]);
+      integrate_face(Fm0, &fbuf[(((long)f * 2 + 1) * 2 + 0) * nn], hs);
+      integrate_face(Fm1, &fbuf[(((long)f * 2 + 1) * 2 + 1) * nn], hs);
     }
 #pragma omp parallel for
     for (int f = 0; f < nb; ++f) {
@@ -686,17 +708,18 @@ struct Oracle {
     for (int f = 0; f < nf; ++f) {
       const int cp = inner[5 * f], fp = inner[5 * f + 1];
       const int cm = inner[5 * f + 2], fm = inner[5 * f + 3];
+      const int hs = inner[5 * f + 4] - 1;  // subface of the "-" side, -1 conforming
       double rp[3][16], rm[3][16], uxp[3][16], uxm[3][16], uzp[3][16], uzm[3][16],
           pp_[3][16], pm[3][16];
       for (int j = 0; j < nst; ++j) {
         eval_face(tile(src[3 * j], cp, 1, 0), fp, rp[j]);
-        eval_face(tile(src[3 * j], cm, 1, 0), fm, rm[j]);
+        eval_face(tile(src[3 * j], cm, 1, 0), fm, rm[j], hs);
         eval_face(tile(src[3 * j + 1], cp, 2, 0), fp, uxp[j]);
-        eval_face(tile(src[3 * j + 1], cm, 2, 0), fm, uxm[j]);
+        eval_face(tile(src[3 * j + 1], cm, 2, 0), fm, uxm[j], hs);
         eval_face(tile(src[3 * j + 1], cp, 2, 1), fp, uzp[j]);
-        eval_face(tile(src[3 * j + 1], cm, 2, 1), fm, uzm[j]);
+        eval_face(tile(src[3 * j + 1], cm, 2, 1), fm, uzm[j], hs);
         eval_face(tile(src[3 * j + 2], cp, 1, 0), fp, pp_[j]);
-        eval_face(tile(src[3 * j + 2], cm, 1, 0), fm, pm[j]);
+        eval_face(tile(src[3 * j + 2], cm, 1, 0), fm, pm[j], hs);
       }
       double Fp[16], Fm[16];
       for (int q = 0; q < nq; ++q) {
@@ -738,7 +761,7 @@ struct Oracle {
         Fm[q] = flux * jxw;
       }
       integrate_face(Fp, &fbuf[((long)f * 2 + 0) * nn]);
-      integrate_face(Fm, &fbuf[((long)f * 2 + 1) * nn]);
+      integrate_face(Fm, &fbuf[((long)f * 2 + 1) * nn], hs);
     }
     gather_faces(dst, 1);
   }
@@ -765,9 +788,10 @@ struct Oracle {
     for (int f = 0; f < nf; ++f) {
       const int cp = inner[5 * f], fp = inner[5 * f + 1];
       const int cm = inner[5 * f + 2], fm = inner[5 * f + 3];
+      const int hs = inner[5 * f + 4] - 1;  // subface of the "-" side, -1 conforming
       double pp_[16], pm[16];
       eval_face(tile(src, cp, 1, 0), fp, pp_);
-      eval_face(tile(src, cm, 1, 0), fm, pm);
+      eval_face(tile(src, cm, 1, 0), fm, pm, hs);
       double Fp0[16], Fp1[16], Fm0[16], Fm1[16];
       for (int q = 0; q < nq; ++q) {
         const double n0 = fN[((long)f * nq + q) * 2], n1 = fN[((long)f * nq + q) * 2 + 1];
@@ -778,8 +802,8 @@ struct Oracle {
       }
       integrate_face(Fp0, &fbuf[(((long)f * 2 + 0) * 2 + 0) * nn]);
       integrate_face(Fp1, &fbuf[(((long)f * 2 + 0) * 2 + 1) * nn]);
-      integrate_face(Fm0, &fbuf[(((long)f * 2 + 1) * 2 + 0) * nn]);
-      integrate_face(Fm1, &fbuf[(((long)f * 2 + 1) * 2 + 1) * nn]);
+      integrate_face(Fm0, &fbuf[(((long)f * 2 + 1) * 2 + 0) * nn], hs);
+      integrate_face(Fm1, &fbuf[(((long)f * 2 + 1) * 2 + 1) * nn], hs);
     }
 #pragma omp parallel for
     for (int f = 0; f < nb; ++f) {
@@ -823,13 +847,14 @@ struct Oracle {
     for (int f = 0; f < nf; ++f) {
       const int cp = inner[5 * f], fp = inner[5 * f + 1];
       const int cm = inner[5 * f + 2], fm = inner[5 * f + 3];
+      const int hs = inner[5 * f + 4] - 1;  // subface of the "-" side, -1 conforming
       double pfp[16], pfm[16], wxp[16], wxm[16], wzp[16], wzm[16];
       eval_face(tile(pres_fixed.data(), cp, 1, 0), fp, pfp);
-      eval_face(tile(pres_fixed.data(), cm, 1, 0), fm, pfm);
+      eval_face(tile(pres_fixed.data(), cm, 1, 0), fm, pfm, hs);
       eval_face(tile(src, cp, 2, 0), fp, wxp);
-      eval_face(tile(src, cm, 2, 0), fm, wxm);
+      eval_face(tile(src, cm, 2, 0), fm, wxm, hs);
       eval_face(tile(src, cp, 2, 1), fp, wzp);
-      eval_face(tile(src, cm, 2, 1), fm, wzm);
+      eval_face(tile(src, cm, 2, 1), fm, wzm, hs);
       double Fp[16], Fm[16];
       for (int q = 0; q < nq; ++q) {
         const double n0 = fN[((long)f * nq + q) * 2], n1 = fN[((long)f * nq + q) * 2 + 1];
@@ -844,7 +869,7 @@ struct Oracle {
         Fm[q] = -flux * jxw;
       }
       integrate_face(Fp, &fbuf[((long)f * 2 + 0) * nn]);
-      integrate_face(Fm, &fbuf[((long)f * 2 + 1) * nn]);
+      integrate_face(Fm, &fbuf[((long)f * 2 + 1) * nn], hs);
     }
     gather_faces(dst, 1);
   }

@@ -1,0 +1,217 @@
+"""Adaptive meshes with hanging faces: the quadtree, its face tables and
+geometry, the solution transfer, and the oracle's discrete identities on
+2:1 meshes (no GPU).  The sm_103a kernels on the same meshes are compared
+with the oracle in test_gpu_operators.py / test_gpu_amr.py."""
+import numpy as np
+import pytest
+
+from atmospheric_flows_gb300 import amr
+from atmospheric_flows_gb300.hill import HillParams, build_case, build_mesh, map_points
+from oracle.oracle import OracleOperator
+
+
+def rel(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def perturbed(case, seed=1, amp=0.01):
+    rng = np.random.default_rng(seed)
+    rho = case.rho * (1 + amp * rng.standard_normal(case.rho.shape))
+    u = case.u + 2.0 * rng.standard_normal(case.u.shape)
+    p = case.p * (1 + amp * rng.standard_normal(case.p.shape))
+    return rho, u, p
+
+
+@pytest.fixture(scope="module")
+def hill_amr():
+    p = HillParams(nx=6, nz=4, degree=3, cfl=2.0)
+    return amr.adaptive_case(p, amr.example_tree(p.nx, p.nz))
+
+
+@pytest.fixture(scope="module")
+def flat_amr():
+    p = HillParams(nx=6, nz=3, degree=3, h0=0.0, cfl=1.0)
+    return amr.adaptive_case(p, amr.example_tree(p.nx, p.nz))
+
+
+def test_balance_and_face_coverage():
+    rng = np.random.default_rng(0)
+    for periodic in (True, False):
+        t = amr.QuadTree(7, 4, periodic, max_level=2)
+        for _ in range(3):
+            leaves = t.leaves()
+            t.refine([leaves[i] for i in rng.choice(len(leaves), 6, replace=False)])
+        t.balance()
+        assert t.is_balanced()
+        inner, bdry = t.face_tables()
+        n = len(t.leaves())
+        # every cell face appears exactly once, except a coarse hanging face twice
+        count = np.zeros((n, 4), dtype=int)
+        for c_p, f_p, c_m, f_m, o in inner:
+            count[c_p, f_p] += 1
+            count[c_m, f_m] += 1
+        for c, f, _ in bdry:
+            count[c, f] += 1
+        coarse = {(c_m, f_m) for c_p, f_p, c_m, f_m, o in inner if o > 0}
+        for c in range(n):
+            for f in range(4):
+                assert count[c, f] == (2 if (c, f) in coarse else 1)
+        # both subfaces of every coarse face are listed, with distinct fine cells
+        for (c, f) in coarse:
+            subs = sorted(o for c_p, f_p, c_m, f_m, o in inner if (c_m, f_m) == (c, f) and o)
+            assert subs == [1, 2]
+
+
+def test_uniform_tree_reproduces_uniform_mesh():
+    p = HillParams(nx=5, nz=3, degree=2)
+    t = amr.QuadTree(p.nx, p.nz, True)
+    inner, bdry = t.face_tables()
+    nodes, inner_u, bdry_u = build_mesh(p)
+    assert sorted(map(tuple, inner)) == sorted(map(tuple, inner_u))
+    assert sorted(map(tuple, bdry)) == sorted(map(tuple, bdry_u))
+    assert np.allclose(amr.leaf_mapping_nodes(t, nodes, p.mapping_degree), nodes, atol=1e-9)
+
+
+def test_hanging_faces_are_geometrically_conforming(hill_amr):
+    """The fine face's points coincide with the coarse face's subface points."""
+    case = hill_amr
+    m = case.params.mapping_degree
+    t = np.linspace(0.0, 1.0, 5)
+    for c_p, f_p, c_m, f_m, o in case.inner_faces:
+        if o == 0:
+            continue
+        s = o - 1
+
+        def face_pts(cell, f, params):
+            pts = np.zeros((len(params), 2))
+            ref = [(0.0, z) if f == 0 else (1.0, z) if f == 1 else (z, 0.0) if f == 2 else (z, 1.0)
+                   for z in params]
+            from atmospheric_flows_gb300.hill import gll_points, lagrange_matrix
+            g = gll_points(m)
+            X = case.mapping_nodes[cell].reshape(m + 1, m + 1, 2)
+            for i, (xi, eta) in enumerate(ref):
+                La = lagrange_matrix(g, np.array([xi]))[0]
+                Lb = lagrange_matrix(g, np.array([eta]))[0]
+                pts[i] = np.einsum("b,a,bad->d", Lb, La, X)
+            return pts
+
+        a = face_pts(c_p, f_p, t)
+        b = face_pts(c_m, f_m, 0.5 * (t + s))
+        if f_p in (0, 1) and abs(a[0, 0] - b[0, 0]) > 1e3:  # periodic seam: shift by the period
+            b[:, 0] += np.round((a[0, 0] - b[0, 0]) / 40000.0) * 40000.0
+        assert np.max(np.abs(a - b)) < 1e-6
+
+
+def test_transfer_refine_then_coarsen_is_identity_and_conservative():
+    p = HillParams(nx=4, nz=3, degree=3, theta_noise=0.1, seed=5)
+    uni = build_case(p)
+    base = build_mesh(p)[0]
+    t0 = amr.QuadTree(p.nx, p.nz, True)
+    t1 = amr.example_tree(p.nx, p.nz)
+    nn2 = (p.degree + 1) ** 2
+    fields = [uni.rho.reshape(-1, 1, nn2), uni.p.reshape(-1, 1, nn2)]
+    fine = amr.transfer_state(t0, t1, base, fields, p.degree, p.mapping_degree)
+    back = amr.transfer_state(t1, t0, base, fine, p.degree, p.mapping_degree)
+    for a, b in zip(back, fields):
+        assert rel(a, b) < 1e-12
+    c1 = amr.adaptive_case(p, t1, state=(fine[0].reshape(-1), uni.u, fine[1].reshape(-1)))
+    m_uni = OracleOperator(uni)
+    m_uni.set_stage(1, 1)
+    m_fine = OracleOperator(c1)
+    m_fine.set_stage(1, 1)
+    m0 = m_uni.vmult(uni.rho).sum()
+    assert abs(m_fine.vmult(c1.rho).sum() - m0) / m0 < 1e-13
+
+
+def test_coarsening_projection_conserves_mass():
+    """Children with independent (non-polynomial) data -> parent: the discrete
+    mass is the same before and after."""
+    p = HillParams(nx=4, nz=3, degree=2, theta_noise=0.1, seed=6)
+    base = build_mesh(p)[0]
+    t1 = amr.example_tree(p.nx, p.nz)
+    c1 = amr.adaptive_case(p, t1)
+    rng = np.random.default_rng(2)
+    rho = c1.rho * (1 + 0.05 * rng.standard_normal(c1.rho.shape))
+    nn2 = (p.degree + 1) ** 2
+    t0 = amr.QuadTree(p.nx, p.nz, True)
+    coarse = amr.transfer_state(t1, t0, base, [rho.reshape(-1, 1, nn2)], p.degree,
+                                p.mapping_degree)[0].reshape(-1)
+    o1 = OracleOperator(c1)
+    o1.set_stage(1, 1)
+    c0 = build_case(p)
+    o0 = OracleOperator(c0)
+    o0.set_stage(1, 1)
+    assert abs(o0.vmult(coarse).sum() - o1.vmult(rho).sum()) / o1.vmult(rho).sum() < 1e-13
+
+
+@pytest.mark.parametrize("stage", [1, 2, 3])
+def test_oracle_rho_rhs_conserves_mass_amr(hill_amr, stage):
+    op = OracleOperator(hill_amr)
+    op.set_stage(stage, 1)
+    rho, u, p = perturbed(hill_amr)
+    src = []
+    for j in range(stage):
+        src += [rho * (1 + 0.1 * j), u * (1 - 0.2 * j)]
+    r = op.vmult_rhs_rho_update(src)
+    m = op.vmult(rho)
+    assert abs(r.sum() - m.sum()) / abs(m.sum()) < 1e-13
+
+
+def test_oracle_rest_states_amr(hill_amr):
+    op = OracleOperator(hill_amr)
+    rho, _, p = perturbed(hill_amr)
+    z = np.zeros(2 * op.n_scalar)
+    op.set_stage(1, 1)
+    assert rel(op.vmult_rhs_rho_update([rho, z]), op.vmult(rho)) < 1e-14
+    op.set_stage(1, 6)
+    assert rel(op.vmult_rhs_pressure([rho, z, p, rho, z]), op.vmult(p)) < 1e-13
+
+
+def test_oracle_momentum_constant_pressure_amr(flat_amr):
+    op = OracleOperator(flat_amr)
+    op.set_params(flat_amr.dt, flat_amr.Ma, 1e30)
+    n = op.n_scalar
+    z = np.zeros(2 * n)
+    p = np.full(n, 0.8)
+    op.set_stage(1, 3)
+    r = op.vmult_rhs_velocity_fixed([np.ones(n), z, p, np.ones(n)])
+    scale = flat_amr.dt / flat_amr.Ma ** 2 * 0.8 * 1e4
+    assert np.max(np.abs(r)) / scale < 1e-12
+
+
+def test_oracle_B_C_integration_by_parts_amr(flat_amr):
+    op = OracleOperator(flat_amr)
+    rng = np.random.default_rng(3)
+    n = op.n_scalar
+    pf = 0.9
+    op.set_pres_fixed(np.full(n, pf))
+    for hs in (1, 2):
+        op.set_stage(hs, 2)
+        q = rng.standard_normal(n)
+        w = rng.standard_normal(2 * n)
+        lhs = np.dot(op.vmult_pressure(q), w) * flat_amr.Ma ** 2
+        rhs = -np.dot(op.vmult_enthalpy(w), q) / (1.4 / 0.4 * pf)
+        assert abs(lhs - rhs) / abs(lhs) < 1e-11
+
+
+def test_indicator_and_marking():
+    p = HillParams(nx=8, nz=4, degree=3, theta_noise=0.1, seed=7)
+    uni = build_case(p)
+    nn2 = (p.degree + 1) ** 2
+    ind = amr.theta_perturbation_gradient(p, uni.mapping_nodes, uni.rho.reshape(-1, nn2),
+                                          uni.p.reshape(-1, nn2))
+    assert ind.shape == (uni.n_cells,) and np.all(ind > 0)
+    # without noise the background is hydrostatic with theta' = 0 (up to the
+    # interpolation of the background)
+    q = HillParams(nx=8, nz=4, degree=3)
+    c0 = build_case(q)
+    ind0 = amr.theta_perturbation_gradient(q, c0.mapping_nodes, c0.rho.reshape(-1, nn2),
+                                           c0.p.reshape(-1, nn2))
+    assert np.max(ind0) < 1e-2 * np.min(ind)
+    t = amr.QuadTree(p.nx, p.nz, True, 2)
+    t1 = amr.mark(t, ind, amr.AdaptParams())
+    assert t1.is_balanced()
+    # one pass from a uniform mesh: exactly the cells above the 90% quantile
+    refined = {iz * p.nx + ix for (l, ix, iz) in t1.refined if l == 0}
+    assert refined == set(np.nonzero(ind > np.quantile(ind, 0.9))[0].tolist())
+    assert len(t1.leaves()) == p.nx * p.nz + 3 * len(refined)

@@ -45,15 +45,32 @@ CASES = [
     dict(nx=6, nz=4, degree=4),
     dict(nx=3, nz=2, degree=5),
     dict(nx=4, nz=3, degree=4, periodic=False),
+    # 2:1 adaptive meshes with hanging faces (periodic seam, walls, 2 levels)
+    dict(nx=6, nz=4, degree=3, amr=True),
+    dict(nx=5, nz=3, degree=2, amr=True),
+    dict(nx=4, nz=3, degree=4, periodic=False, amr=True),
+    dict(nx=4, nz=2, degree=1, amr=True),
 ]
 
 
+def make_case(d):
+    d = dict(d)
+    adaptive = d.pop("amr", False)
+    p = HillParams(cfl=3.0, **d)
+    if not adaptive:
+        return build_case(p)
+    from atmospheric_flows_gb300 import amr
+
+    return amr.adaptive_case(p, amr.example_tree(p.nx, p.nz, p.periodic))
+
+
 @pytest.fixture(scope="module", params=CASES, ids=lambda d: "k{degree}_{nx}x{nz}".format(**d)
-                + ("_walls" if not d.get("periodic", True) else ""))
+                + ("_walls" if not d.get("periodic", True) else "")
+                + ("_amr" if d.get("amr") else ""))
 def pair(request, cuda_ok):
     from atmospheric_flows_gb300.euler_operator import EULEROperator, MatrixFreeStorage
 
-    case = build_case(HillParams(cfl=3.0, **request.param))
+    case = make_case(request.param)
     g = EULEROperator(MatrixFreeStorage.from_case(case), case.dt, case.Ma, case.Fr)
     o = OracleOperator(case)
     return case, g, o
