@@ -214,18 +214,21 @@ def leaf_mapping_nodes(tree: QuadTree, base_nodes: np.ndarray, m: int) -> np.nda
     """Mapping nodes of every leaf: its base cell's mapping at the leaf's
     sub-square GLL points.  Returns [n_leaves, (m+1)^2, 2]."""
     ref = gll_points(m)
-    leaves = tree.leaves()
+    leaves = np.asarray(tree.leaves(), dtype=np.int64).reshape(-1, 3)
     out = np.empty((len(leaves), (m + 1) ** 2, 2))
     base = base_nodes.reshape(base_nodes.shape[0], m + 1, m + 1, 2)
-    for i, (l, ix, iz) in enumerate(leaves):
-        h = 1.0 / (1 << l)
-        bx, bz = ix >> l, iz >> l
-        a0 = (ix - (bx << l)) * h
-        b0 = (iz - (bz << l)) * h
-        La = lagrange_matrix(ref, a0 + h * ref)
-        Lb = lagrange_matrix(ref, b0 + h * ref)
-        c = bz * tree.nx + bx
-        out[i] = np.einsum("zb,xa,bad->zxd", Lb, La, base[c]).reshape(-1, 2)
+    l, ix, iz = leaves[:, 0], leaves[:, 1], leaves[:, 2]
+    bx, bz = ix >> l, iz >> l
+    ox, oz = ix - (bx << l), iz - (bz << l)
+    cell = bz * tree.nx + bx
+    key = (l * 64 + ox) * 64 + oz
+    for kv in np.unique(key):
+        sel = np.nonzero(key == kv)[0]
+        lv, a, b = int(l[sel[0]]), int(ox[sel[0]]), int(oz[sel[0]])
+        h = 1.0 / (1 << lv)
+        La = lagrange_matrix(ref, a * h + h * ref)
+        Lb = lagrange_matrix(ref, b * h + h * ref)
+        out[sel] = np.einsum("zb,xa,cbad->czxd", Lb, La, base[cell[sel]]).reshape(len(sel), -1, 2)
     return out
 
 
@@ -286,42 +289,69 @@ def _restrict_cell(children, child_nodes, parent_nodes, k, m):
 
 def transfer_state(old: QuadTree, new: QuadTree, base_nodes, fields, k, m):
     """Move nodal fields ([n_old_leaves, ncomp, nn2] each) from `old` leaves
-    to `new` leaves.  Leaves present in both are copied; refined leaves are
-    interpolated (repeatedly for several levels); coarsened parents are L2
-    projections of their children (recursively)."""
+    to `new` leaves.  Leaves present in both are copied; leaves below an old
+    leaf are interpolated from it (one matrix per depth and position, applied
+    to all such leaves at once); leaves above old leaves are L2 projections of
+    their children (recursively)."""
     oidx = old.leaf_index()
-    nn2 = (k + 1) ** 2
-    # values of any node of the old tree, by interpolation from an ancestor leaf
-    cache = {}
-
-    def value_of(node, f):
-        key = (node, f)
-        if key in cache:
-            return cache[key]
+    nn = k + 1
+    nn2 = nn * nn
+    new_leaves = new.leaves()
+    out = [np.empty((len(new_leaves),) + f.shape[1:]) for f in fields]
+    P1 = _prolong_1d(k)
+    groups = {}  # (depth, ox, oz) -> (new positions, old leaf indices)
+    coarser = []
+    for j, node in enumerate(new_leaves):
         if node in oidx:
-            v = fields[f][oidx[node]]
-        elif node in old.refined:  # coarser than the old leaves: project
-            l, ix, iz = node
-            kids = [(l + 1, 2 * ix + a, 2 * iz + b) for b in range(2) for a in range(2)]
-            vals = [value_of(kn, f) for kn in kids]
-            v = _restrict_cell(vals, [node_geometry(kn) for kn in kids],
-                               node_geometry(node), k, m)
-        else:  # finer than the old leaves: interpolate from the parent
-            l, ix, iz = node
-            parent = (l - 1, ix >> 1, iz >> 1)
-            v = prolong_cell(value_of(parent, f), k)[(ix & 1) + 2 * (iz & 1)]
-        cache[key] = v
-        return v
+            groups.setdefault((0, 0, 0), ([], []))
+            g = groups[(0, 0, 0)]
+            g[0].append(j)
+            g[1].append(oidx[node])
+            continue
+        l, ix, iz = node
+        found = None
+        for d in range(1, l + 1):
+            anc = (l - d, ix >> d, iz >> d)
+            if anc in oidx:
+                found = (d, ix - (anc[1] << d), iz - (anc[2] << d), oidx[anc])
+                break
+        if found is None:
+            coarser.append((j, node))
+            continue
+        d, ox, oz, oi = found
+        g = groups.setdefault((d, ox, oz), ([], []))
+        g[0].append(j)
+        g[1].append(oi)
+    for (d, ox, oz), (js, ois) in groups.items():
+        Px, Pz = np.eye(nn), np.eye(nn)
+        for t in range(d):  # from the ancestor down: bit d-1-t of the offset
+            Px = P1[(ox >> (d - 1 - t)) & 1] @ Px
+            Pz = P1[(oz >> (d - 1 - t)) & 1] @ Pz
+        js, ois = np.asarray(js), np.asarray(ois)
+        for f, arr in enumerate(fields):
+            U = arr[ois].reshape(len(ois), -1, nn, nn)
+            out[f][js] = np.einsum("zj,xi,cnji->cnzx", Pz, Px, U).reshape(len(ois), -1, nn2)
+
+    geo = {}
 
     def node_geometry(node):
-        t = QuadTree(old.nx, old.nz, old.periodic, old.max_level)
-        t._leaves = [node]
-        return leaf_mapping_nodes(t, base_nodes, m)[0]
+        if node not in geo:
+            t = QuadTree(old.nx, old.nz, old.periodic, old.max_level)
+            t._leaves = [node]
+            geo[node] = leaf_mapping_nodes(t, base_nodes, m)[0]
+        return geo[node]
 
-    out = []
-    for f in range(len(fields)):
-        arr = np.stack([value_of(leaf, f) for leaf in new.leaves()])
-        out.append(arr.reshape(len(new.leaves()), -1, nn2))
+    def value_of(node, f):
+        if node in oidx:
+            return fields[f][oidx[node]]
+        l, ix, iz = node
+        kids = [(l + 1, 2 * ix + a, 2 * iz + b) for b in range(2) for a in range(2)]
+        vals = [value_of(kn, f) for kn in kids]
+        return _restrict_cell(vals, [node_geometry(kn) for kn in kids], node_geometry(node), k, m)
+
+    for j, node in coarser:
+        for f in range(len(fields)):
+            out[f][j] = value_of(node, f)
     return out
 
 
