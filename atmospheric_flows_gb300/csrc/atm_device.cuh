@@ -30,9 +30,12 @@ struct Cfg {
 
 // [degree][w][q*(k+1)+i]: w = 0 values and 1 derivatives at the 2k+1 Gauss
 // points g_q; w = 2, 3 values at the subface points (g_q + s)/2, s = 0, 1, of
-// a hanging face.  Each translation unit holds its own copy in its constant
+// a hanging face; w = 4..7 the even/odd halves of the value and derivative
+// tables for q < k, i < (k+1)/2 (E = (S(q,i) + S(q,k-i))/2,
+// O = (S(q,i) - S(q,k-i))/2, same for D), used by the even-odd
+// contractions.  Each translation unit holds its own copy in its constant
 // bank.
-constexpr int BASIS_TABLES = 4;
+constexpr int BASIS_TABLES = 8;
 static __constant__ double c_basis[KMAX + 1][BASIS_TABLES][NQ_MAX * NN_MAX];
 static __constant__ float c_basis_f[KMAX + 1][BASIS_TABLES][NQ_MAX * NN_MAX];
 
@@ -58,6 +61,11 @@ template <int K, typename T = double>
 __device__ __forceinline__ T bS(int q, int i) { return CBasis<T>::get(K, 0, q * (K + 1) + i); }
 template <int K, typename T = double>
 __device__ __forceinline__ T bD(int q, int i) { return CBasis<T>::get(K, 1, q * (K + 1) + i); }
+// even/odd halves (q < K, i < (K+1)/2): w = 4 E_S, 5 O_S, 6 E_D, 7 O_D
+template <int K, typename T = double>
+__device__ __forceinline__ T bEO(int w, int q, int i) {
+  return CBasis<T>::get(K, w, q * (K + 1) + i);
+}
 // value of basis function i at point q of subface s of a hanging face
 template <int K, typename T = double>
 __device__ __forceinline__ T bH(int s, int q, int i) {
@@ -93,11 +101,16 @@ __device__ __forceinline__ void load_cols(int t, T (&St)[2 * K + 1], T (&Dt)[2 *
   }
 }
 
-// values of a nodal tile on the thread's quadrature column
+// values of a nodal tile on the thread's quadrature column.  The
+// z-contraction uses the even-odd split of the symmetric point sets
+// (S(2k-q, k-i) = S(q, i)): for the pair (q, 2k-q) it forms
+//   e = sum_i E(q,i) (t_i + t_{k-i}) [+ S(q,k/2) t_{k/2}],
+//   o = sum_i O(q,i) (t_i - t_{k-i}),   v_q = e + o,  v_{2k-q} = e - o.
 template <int K, typename T>
 __device__ __forceinline__ void eval_col(const T *__restrict__ tile, const T (&Sx)[K + 1],
                                          T (&v)[2 * K + 1]) {
-  constexpr int NN = K + 1, NQ = 2 * K + 1;
+  constexpr int NN = K + 1, NQ = 2 * K + 1, H = NN / 2;
+  constexpr bool MID = (NN & 1) != 0;
   T t[NN];
 #pragma unroll
   for (int iz = 0; iz < NN; ++iz) {
@@ -106,36 +119,105 @@ __device__ __forceinline__ void eval_col(const T *__restrict__ tile, const T (&S
     for (int ix = 0; ix < NN; ++ix) s = fma(Sx[ix], tile[iz * NN + ix], s);
     t[iz] = s;
   }
+  T te[H > 0 ? H : 1], to[H > 0 ? H : 1];
 #pragma unroll
-  for (int qz = 0; qz < NQ; ++qz) {
-    T s = 0;
+  for (int i = 0; i < H; ++i) {
+    te[i] = t[i] + t[K - i];
+    to[i] = t[i] - t[K - i];
+  }
 #pragma unroll
-    for (int iz = 0; iz < NN; ++iz) s = fma(bS<K, T>(qz, iz), t[iz], s);
-    v[qz] = s;
+  for (int q = 0; q < K; ++q) {
+    T e = MID ? bS<K, T>(q, H) * t[H] : T(0);
+    T o = 0;
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+      e = fma(bEO<K, T>(4, q, i), te[i], e);
+      o = fma(bEO<K, T>(5, q, i), to[i], o);
+    }
+    v[q] = e + o;
+    v[NQ - 1 - q] = e - o;
+  }
+  {
+    T e = MID ? bS<K, T>(K, H) * t[H] : T(0);
+#pragma unroll
+    for (int i = 0; i < H; ++i) e = fma(bS<K, T>(K, i), te[i], e);
+    v[K] = e;
   }
 }
 
 // z-contraction of the submitted quantities of one column:
 //   xa[iz][col] = sum_qz S(qz,iz) V + D(qz,iz) Geta ;  xb[iz][col] = sum_qz S(qz,iz) Gxi
-// V, Gxi, Geta already carry JxW and the inverse Jacobian.
+// V, Gxi, Geta already carry JxW and the inverse Jacobian.  Even-odd split
+// over the point pairs (q, 2k-q) and the output pairs (i, k-i); D is
+// antisymmetric (D(2k-q, k-i) = -D(q, i)):
+//   e = sum_q E_S (V_q + V_q') + E_D (G_q - G_q') [+ S(k,i) V_k]
+//   o = sum_q O_S (V_q - V_q') + O_D (G_q + G_q') [+ D(k,i) G_k]
+//   out_i = e + o,  out_{k-i} = e - o.
 template <int K, bool HAS_V, bool HAS_G, typename T>
 __device__ __forceinline__ void integrate_col_z(const T (&V)[2 * K + 1], const T (&Gxi)[2 * K + 1],
                                                 const T (&Get)[2 * K + 1], T *__restrict__ xa,
                                                 T *__restrict__ xb, int col) {
-  constexpr int NN = K + 1, NQ = 2 * K + 1;
+  constexpr int NN = K + 1, NQ = 2 * K + 1, H = NN / 2;
+  constexpr bool MID = (NN & 1) != 0;
+  T ve[K], vo[K], ge[K], go[K], xe[K], xo[K];
 #pragma unroll
-  for (int iz = 0; iz < NN; ++iz) {
-    T sa = 0, sb = 0;
+  for (int q = 0; q < K; ++q) {
+    if (HAS_V) {
+      ve[q] = V[q] + V[NQ - 1 - q];
+      vo[q] = V[q] - V[NQ - 1 - q];
+    }
+    if (HAS_G) {
+      ge[q] = Get[q] + Get[NQ - 1 - q];
+      go[q] = Get[q] - Get[NQ - 1 - q];
+      xe[q] = Gxi[q] + Gxi[NQ - 1 - q];
+      xo[q] = Gxi[q] - Gxi[NQ - 1 - q];
+    }
+  }
 #pragma unroll
-    for (int qz = 0; qz < NQ; ++qz) {
-      if (HAS_V) sa = fma(bS<K, T>(qz, iz), V[qz], sa);
+  for (int i = 0; i < H; ++i) {
+    T e = 0, o = 0;
+    if (HAS_V) e = bS<K, T>(K, i) * V[K];
+    if (HAS_G) o = bD<K, T>(K, i) * Get[K];
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      if (HAS_V) {
+        e = fma(bEO<K, T>(4, q, i), ve[q], e);
+        o = fma(bEO<K, T>(5, q, i), vo[q], o);
+      }
       if (HAS_G) {
-        sa = fma(bD<K, T>(qz, iz), Get[qz], sa);
-        sb = fma(bS<K, T>(qz, iz), Gxi[qz], sb);
+        e = fma(bEO<K, T>(6, q, i), go[q], e);
+        o = fma(bEO<K, T>(7, q, i), ge[q], o);
       }
     }
-    xa[iz * NQ + col] = sa;
-    if (HAS_G) xb[iz * NQ + col] = sb;
+    xa[i * NQ + col] = e + o;
+    xa[(K - i) * NQ + col] = e - o;
+    if (HAS_G) {
+      T eb = bS<K, T>(K, i) * Gxi[K], ob = 0;
+#pragma unroll
+      for (int q = 0; q < K; ++q) {
+        eb = fma(bEO<K, T>(4, q, i), xe[q], eb);
+        ob = fma(bEO<K, T>(5, q, i), xo[q], ob);
+      }
+      xb[i * NQ + col] = eb + ob;
+      xb[(K - i) * NQ + col] = eb - ob;
+    }
+  }
+  if (MID) {
+    // i = k/2: O_S = O_D = 0 and D(k, k/2) = 0
+    T e = 0;
+    if (HAS_V) e = bS<K, T>(K, H) * V[K];
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      if (HAS_V) e = fma(bS<K, T>(q, H), ve[q], e);
+      if (HAS_G) e = fma(bD<K, T>(q, H), go[q], e);
+    }
+    xa[H * NQ + col] = e;
+    if (HAS_G) {
+      T eb = bS<K, T>(K, H) * Gxi[K];
+#pragma unroll
+      for (int q = 0; q < K; ++q) eb = fma(bS<K, T>(q, H), xe[q], eb);
+      xb[H * NQ + col] = eb;
+    }
   }
 }
 

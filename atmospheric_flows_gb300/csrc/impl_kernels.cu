@@ -132,76 +132,132 @@ __global__ void __launch_bounds__(Cfg<K>::THREADS)
 }
 
 // ================================================= exact block inverse ===
-// One warp per cell: assemble the (weighted) cell mass matrix by sum
-// factorisation, invert it in place by Gauss-Jordan elimination (SPD, no
-// pivoting) and store it transposed.
+// One warp per cell.  The (weighted) cell mass matrix
+//   M[(iz,ix),(jz,jx)] = sum_q S(qz,iz)S(qz,jz) S(qx,ix)S(qx,jx) w(q) JxW(q)
+// is symmetric positive definite: only its lower triangle is assembled, in
+// packed storage, by sum factorisation over the symmetric 1D index pairs
+// (a <= b) with the products S(q,a)S(q,b) tabulated once per block.  It is
+// then inverted in place by the symmetric sweep operator (Gauss-Jordan
+// restricted to the lower triangle; SPD, no pivoting), which leaves -M^{-1}.
+// The inverse is written out in full, transposed (it is symmetric).
 constexpr int BI_WARPS = 2;
+
+template <int K>
+struct BlockInvCfg {
+  static constexpr int NN = K + 1, NQ = 2 * K + 1, NN2 = NN * NN, NQ2 = NQ * NQ;
+  static constexpr int NP = NN * (NN + 1) / 2;        // 1D pairs a <= b
+  static constexpr int NTRI = NN2 * (NN2 + 1) / 2;    // packed lower triangle
+  static constexpr int PER = NQ2 + NQ * NP + NTRI + 2 * NN2 + NN * NQ;  // per warp
+  // block tables: S products [NQ][NP], then byte tables of pair/triangle indices
+  static constexpr int TAB_BYTES = ((NQ * NP) * 8 + 2 * NTRI + 7) / 8 * 8;
+  template <typename T>
+  static size_t smem() { return TAB_BYTES + sizeof(T) * (size_t)BI_WARPS * PER; }
+};
+
+__device__ __forceinline__ int tri_index(int i, int j) {  // i >= j
+  return i * (i + 1) / 2 + j;
+}
+__device__ __forceinline__ int sym_index(int i, int j) {
+  return i >= j ? tri_index(i, j) : tri_index(j, i);
+}
+
 template <int K, typename T>
 __global__ void __launch_bounds__(32 * BI_WARPS)
     k_block_inverse(T *__restrict__ out, const T *__restrict__ weight, MeshT<T> mesh) {
-  constexpr int NN = K + 1, NQ = 2 * K + 1, NN2 = NN * NN, NQ2 = NQ * NQ;
-  constexpr int PER = NQ2 + NQ * NN * NN + NN2 * NN2;
+  using B = BlockInvCfg<K>;
+  constexpr int NN = B::NN, NQ = B::NQ, NN2 = B::NN2, NQ2 = B::NQ2, NP = B::NP;
+  constexpr int NTRI = B::NTRI;
   extern __shared__ __align__(16) unsigned char sm_raw[];
-  T *sm = reinterpret_cast<T *>(sm_raw);
+  T *ss = reinterpret_cast<T *>(sm_raw);                              // [NQ][NP]
+  unsigned char *ti = sm_raw + (size_t)NQ * NP * sizeof(T);           // [NTRI] row
+  unsigned char *tj = ti + NTRI;                                      // [NTRI] column
+  T *wsm = reinterpret_cast<T *>(sm_raw + B::TAB_BYTES);
+  // block tables
+  for (int e = threadIdx.x; e < NQ * NP; e += blockDim.x) {
+    const int q = e / NP, p = e - q * NP;
+    int b = 0;
+    while ((b + 1) * (b + 2) / 2 <= p) ++b;
+    const int a = p - b * (b + 1) / 2;
+    ss[e] = bS<K, T>(q, a) * bS<K, T>(q, b);
+  }
+  for (int e = threadIdx.x; e < NTRI; e += blockDim.x) {
+    int i = 0;
+    while ((i + 1) * (i + 2) / 2 <= e) ++i;
+    ti[e] = (unsigned char)i;
+    tj[e] = (unsigned char)(e - i * (i + 1) / 2);
+  }
+  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = blockIdx.x * BI_WARPS + warp;
-  if (c >= mesh.nc) return;  // warp-uniform; no block-wide barriers below
-  T *wq = sm + warp * PER;
-  T *Tb = wq + NQ2;
-  T *M = Tb + NQ * NN * NN;
+  if (c >= mesh.nc) return;  // warp-uniform; only warp-level barriers below
+  T *wq = wsm + warp * B::PER;   // [NQ2] w JxW at the quadrature points
+  T *Tb = wq + NQ2;              // [NQ][NP] x-contracted weights
+  T *M = Tb + NQ * NP;           // [NTRI] packed lower triangle
+  T *colk = M + NTRI;            // [NN2] pivot column
+  T *cd = colk + NN2;            // [NN2] pivot column / pivot
+  T *tx = cd + NN2;              // [NN][NQ] x-contracted weight field
   const T *G = mesh.qgeo + (long)c * 5 * NQ2;
-  for (int q = lane; q < NQ2; q += 32) {
-    const int qz = q / NQ, qx = q - qz * NQ;
-    T wv = T(1.0);
-    if (weight) {
-      const T *wt = weight + (long)c * NN2;
+  if (weight) {
+    const T *wt = weight + (long)c * NN2;
+    for (int e = lane; e < NN * NQ; e += 32) {
+      const int iz = e / NQ, qx = e - iz * NQ;
       T s = T(0.0);
-      for (int iz = 0; iz < NN; ++iz) {
-        T t = T(0.0);
-        for (int ix = 0; ix < NN; ++ix) t = fma(bS<K, T>(qx, ix), wt[iz * NN + ix], t);
-        s = fma(bS<K, T>(qz, iz), t, s);
-      }
-      wv = s;
+#pragma unroll
+      for (int ix = 0; ix < NN; ++ix) s = fma(bS<K, T>(qx, ix), wt[iz * NN + ix], s);
+      tx[e] = s;
     }
-    wq[q] = wv * G[4 * NQ2 + q];
+    __syncwarp();
+    for (int q = lane; q < NQ2; q += 32) {
+      const int qz = q / NQ, qx = q - qz * NQ;
+      T s = T(0.0);
+#pragma unroll
+      for (int iz = 0; iz < NN; ++iz) s = fma(bS<K, T>(qz, iz), tx[iz * NQ + qx], s);
+      wq[q] = s * G[4 * NQ2 + q];
+    }
+  } else {
+    for (int q = lane; q < NQ2; q += 32) wq[q] = G[4 * NQ2 + q];
   }
   __syncwarp();
-  for (int e = lane; e < NQ * NN * NN; e += 32) {
-    const int qz = e / (NN * NN), r = e - qz * NN * NN, ix = r / NN, jx = r - ix * NN;
+  for (int e = lane; e < NQ * NP; e += 32) {
+    const int qz = e / NP, p = e - qz * NP;
     T s = T(0.0);
-    for (int qx = 0; qx < NQ; ++qx) s = fma(bS<K, T>(qx, ix) * bS<K, T>(qx, jx), wq[qz * NQ + qx], s);
+#pragma unroll
+    for (int qx = 0; qx < NQ; ++qx) s = fma(ss[qx * NP + p], wq[qz * NQ + qx], s);
     Tb[e] = s;
   }
   __syncwarp();
-  for (int e = lane; e < NN2 * NN2; e += 32) {
-    const int i = e / NN2, j = e - i * NN2;
-    const int iz = i / NN, ix = i - iz * NN, jz = j / NN, jx = j - jz * NN;
+  for (int e = lane; e < NTRI; e += 32) {
+    const int I = ti[e], J = tj[e];
+    const int iz = I / NN, ix = I - iz * NN, jz = J / NN, jx = J - jz * NN;
+    const int pz = sym_index(iz, jz), px = sym_index(ix, jx);
     T s = T(0.0);
-    for (int qz = 0; qz < NQ; ++qz)
-      s = fma(bS<K, T>(qz, iz) * bS<K, T>(qz, jz), Tb[(qz * NN + ix) * NN + jx], s);
+#pragma unroll
+    for (int qz = 0; qz < NQ; ++qz) s = fma(ss[qz * NP + pz], Tb[qz * NP + px], s);
     M[e] = s;
   }
   __syncwarp();
-  for (int pv = 0; pv < NN2; ++pv) {
-    const T d = T(1.0) / M[pv * NN2 + pv];
-    __syncwarp();
-    for (int j = lane; j < NN2; j += 32)
-      if (j != pv) M[pv * NN2 + j] *= d;
-    __syncwarp();
-    for (int e = lane; e < NN2 * NN2; e += 32) {
-      const int i = e / NN2, j = e - i * NN2;
-      if (i != pv && j != pv) M[e] -= M[i * NN2 + pv] * M[pv * NN2 + j];
+  // symmetric sweep on pivots k = 0..NN2-1:
+  //   a_ij -= a_ik a_kj / a_kk (i, j != k);  a_ik = a_ik / a_kk;  a_kk = -1 / a_kk
+  for (int k = 0; k < NN2; ++k) {
+    const T d = T(1.0) / M[tri_index(k, k)];
+    for (int i = lane; i < NN2; i += 32) {  // NN2 = 36 > 32 for k = 5
+      const T a = M[sym_index(i, k)];
+      colk[i] = a;
+      cd[i] = a * d;
     }
     __syncwarp();
-    for (int i = lane; i < NN2; i += 32)
-      if (i != pv) M[i * NN2 + pv] = -M[i * NN2 + pv] * d;
-    if (lane == 0) M[pv * NN2 + pv] = d;
+    for (int e = lane; e < NTRI; e += 32) {
+      const int i = ti[e], j = tj[e];
+      if (i != k && j != k) M[e] = fma(-cd[i], colk[j], M[e]);
+    }
+    __syncwarp();
+    for (int i = lane; i < NN2; i += 32) M[sym_index(i, k)] = i == k ? -d : cd[i];
     __syncwarp();
   }
   T *o = out + (long)c * NN2 * NN2;
   for (int e = lane; e < NN2 * NN2; e += 32) {
     const int j = e / NN2, i = e - j * NN2;
-    o[e] = M[i * NN2 + j];
+    o[e] = -M[sym_index(i, j)];
   }
 }
 
@@ -252,8 +308,7 @@ int invdiag_launch(const OpView<T> &v, T *out, int ncomp, const T *weight, T sca
 
 template <int K, typename T>
 int block_inverse_launch(const OpView<T> &v, T *out, const T *weight) {
-  constexpr int NN = K + 1, NQ = 2 * K + 1, NN2 = NN * NN, NQ2 = NQ * NQ;
-  const size_t sm = sizeof(T) * BI_WARPS * (NQ2 + NQ * NN * NN + NN2 * NN2);
+  const size_t sm = BlockInvCfg<K>::template smem<T>();
   if (sm > 48 * 1024)
     ATM_CUDA(cudaFuncSetAttribute(k_block_inverse<K, T>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));

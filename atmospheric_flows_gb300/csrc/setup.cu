@@ -111,7 +111,7 @@ int upload_basis_all() {
   if (dev >= 0 && dev < 64 && done[dev]) return ATM_OK;
   // [k][w][q*(k+1)+i]: w = 0 values, 1 derivatives at the Gauss points,
   // 2 and 3 values at the subface points (g_q + s)/2 (hanging faces)
-  constexpr int NW = 4;
+  constexpr int NW = 8;
   std::vector<double> tab((KMAX + 1) * NW * NQ_MAX * NN_MAX, 0.0);
   for (int k = 1; k <= KMAX; ++k) {
     HostBasis b = make_basis(k);
@@ -123,6 +123,18 @@ int upload_basis_all() {
       double *H = &tab[(k * NW + 2 + s) * NQ_MAX * NN_MAX];
       for (int q = 0; q < b.nq; ++q)
         lagrange_eval(b.gll, 0.5 * (b.gauss[q] + s), &H[q * b.nn], nullptr);
+    }
+    // even/odd halves for q < k, i < (k+1)/2 (same [q*(k+1)+i] indexing)
+    for (int w = 0; w < 2; ++w) {
+      const std::vector<double> &src = w == 0 ? b.S : b.D;
+      double *E = &tab[(k * NW + 4 + 2 * w) * NQ_MAX * NN_MAX];
+      double *O = &tab[(k * NW + 5 + 2 * w) * NQ_MAX * NN_MAX];
+      for (int q = 0; q < k; ++q)
+        for (int i = 0; i < b.nn / 2; ++i) {
+          const double a = src[q * b.nn + i], c = src[q * b.nn + k - i];
+          E[q * b.nn + i] = 0.5 * (a + c);
+          O[q * b.nn + i] = 0.5 * (a - c);
+        }
     }
   }
   if (upload_basis_rhs(tab.data()) || upload_basis_impl(tab.data()) ||
