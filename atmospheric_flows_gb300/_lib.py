@@ -54,6 +54,8 @@ SIGNATURES = {
     "atm_mg_add_level": (_i, [_h, _i, _i, _dp, _i, _ip, _i, _ip, _ip]),
     "atm_mg_set_smoother": (_i, [_h, _i, _d, _i, _i]),
     "atm_mg_vcycle": (_i, [_h, _i, ctypes.c_void_p, ctypes.c_void_p]),
+    "atm_mg_set_graphs": (_i, [_h, _i]),
+    "atm_mg_stats": (_i, [_h, ctypes.POINTER(ctypes.c_long)]),
     "atm_solve_fgmres": (_i, [_h, _i, ctypes.c_void_p, ctypes.c_void_p, _d, _i, _ip, _dp]),
     "atm_set_true_residual_check": (_i, [_h, _i]),
     "atm_solver_init": (_i, [_h, _d, _d, _d, _d, _i, _i]),

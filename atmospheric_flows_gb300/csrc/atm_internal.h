@@ -107,6 +107,7 @@ struct atm_ctx {
   // GMRES/FGMRES only stop on a recomputed true residual (S is nonlinear)
   bool true_residual_check = false;
   mutable atm::KTimer timer;
+  bool capturing = false;  // a CUDA graph is being recorded: timers are off
   long n_scalar() const { return (long)nc * nn2; }
   long n_vector() const { return 2L * nc * nn2; }
 };
@@ -239,6 +240,8 @@ int fgmres_mg(atm_ctx &c, int precision, double *x, const double *b, double tol,
               int *its, double *res);
 void mg_mark_rho_changed(atm_ctx &c);
 long mg_vcycles(const atm_ctx &c);
+int mg_set_graphs(atm_ctx &c, bool on);
+void mg_stats(const atm_ctx &c, long *out);
 int mg_levels(const atm_ctx &c);
 
 // ------------------------------------------------------------ mesh set-up --

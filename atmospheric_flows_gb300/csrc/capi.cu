@@ -11,7 +11,7 @@ namespace atm {
 std::atomic<long> g_kernel_launches{0};
 
 TimedRegion::TimedRegion(const atm_ctx &ctx, int family, double bytes, double flops)
-    : c(ctx), slot(0), on(ctx.timer.on) {
+    : c(ctx), slot(0), on(ctx.timer.on && !ctx.capturing) {
   if (!on) return;
   KTimer &t = c.timer;
   if (t.used * 2 + 2 > t.ev.size()) {
@@ -365,6 +365,16 @@ int atm_mg_vcycle(atm_handle h, int precision, double *dst, const double *src) {
   CHECK_PTR(src, "src");
   if (precision != 1 && precision != 2) { set_error("precision must be 1 or 2"); return ATM_BAD_ARG; }
   return mg_precondition(*h, precision, dst, src);
+}
+int atm_mg_set_graphs(atm_handle h, int on) {
+  CHECK_H(h);
+  return mg_set_graphs(*h, on != 0);
+}
+int atm_mg_stats(atm_handle h, long *out) {
+  CHECK_H(h);
+  CHECK_PTR(out, "out");
+  mg_stats(*h, out);
+  return ATM_OK;
 }
 int atm_set_true_residual_check(atm_handle h, int on) {
   CHECK_H(h);

@@ -51,6 +51,14 @@ struct MGHier {
   XferTabT<T> tab;
   bool built = false;
   bool rho_dirty = true;
+  // The V-cycle as a captured CUDA graph.  Its kernel arguments depend on the
+  // implicit coefficient, dt, Ma (level operators) and the eigenvalue
+  // estimates (Chebyshev), so it is re-captured when any of them changes.
+  cudaGraphExec_t graph = nullptr;
+  long graph_kernels = 0;   // kernels in one replay
+  double graph_key[4] = {0, 0, 0, -1};
+  long lam_epoch = 0;       // bumped whenever the eigenvalue estimates change
+  bool graph_failed = false;
 };
 
 struct MG {
@@ -68,6 +76,9 @@ struct MG {
   int restart = 16;
   double *zbasis = nullptr;  // FGMRES preconditioned directions [restart][ns]
   long vcycles = 0;
+  bool use_graphs = true;             // replay the V-cycle as a CUDA graph
+  cudaStream_t cap_stream = nullptr;  // private stream the V-cycle is captured on
+  long graph_replays = 0;
 };
 
 namespace {
@@ -261,11 +272,21 @@ void level_free(MGLevelT<T> &L) {
 }
 
 template <typename T>
+void hier_drop_graph(MGHier<T> &H) {
+  if (H.graph) cudaGraphExecDestroy(H.graph);
+  H.graph = nullptr;
+  H.graph_kernels = 0;
+  H.graph_key[3] = -1;
+}
+
+template <typename T>
 void hier_free(MGHier<T> &H) {
+  hier_drop_graph(H);
   for (auto &L : H.lv) level_free(L);
   H.lv.clear();
   H.built = false;
   H.rho_dirty = true;
+  H.graph_failed = false;
 }
 
 template <typename T>
@@ -491,8 +512,50 @@ int prepare(atm_ctx &c, MG &mg) {
       if ((rc = estimate_lambda<T>(c, L, mg.eig_its))) return rc;
     }
     H.rho_dirty = false;
+    ++H.lam_epoch;
   }
   return ATM_OK;
+}
+
+// Record one V-cycle (input L0.b, output L0.x) into H.graph.  The capture
+// runs on the hierarchy's private non-blocking stream (the legacy default
+// stream cannot be captured) in thread-local mode, so members captured or
+// running on other threads are not affected; the kernels counted while
+// recording did not run and are taken off the launch counter.
+template <typename T>
+int capture_vcycle(atm_ctx &c, MG &mg, MGHier<T> &H) {
+  if (!mg.cap_stream)
+    ATM_CUDA(cudaStreamCreateWithFlags(&mg.cap_stream, cudaStreamNonBlocking));
+  hier_drop_graph(H);
+  // the capture stream must not start before work already queued on c.stream
+  ATM_CUDA(cudaStreamSynchronize(c.stream));
+  cudaStream_t saved = c.stream;
+  c.stream = mg.cap_stream;
+  c.capturing = true;
+  const long before = g_kernel_launches.load();
+  cudaError_t e = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal);
+  int rc = e == cudaSuccess ? ATM_OK : cuda_fail(e, "cudaStreamBeginCapture");
+  if (rc == ATM_OK) {
+    rc = vcycle<T>(c, mg, H, 0);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(c.stream, &g);
+    if (rc == ATM_OK && e != cudaSuccess) rc = cuda_fail(e, "cudaStreamEndCapture");
+    if (rc == ATM_OK) {
+      e = cudaGraphInstantiate(&H.graph, g, 0);
+      if (e != cudaSuccess) {
+        H.graph = nullptr;
+        rc = cuda_fail(e, "cudaGraphInstantiate");
+      }
+    }
+    if (g) cudaGraphDestroy(g);
+  }
+  const long recorded = g_kernel_launches.load() - before;
+  g_kernel_launches.fetch_sub(recorded);
+  c.capturing = false;
+  c.stream = saved;
+  if (rc == ATM_OK) H.graph_kernels = recorded;
+  cudaGetLastError();  // a failed capture leaves no sticky error behind
+  return rc;
 }
 
 template <typename T>
@@ -502,8 +565,27 @@ int precondition(atm_ctx &c, MG &mg, double *z, const double *v) {
   const long n = c.n_scalar();
   k_convert<T, double><<<gsz(n), 256, 0, c.stream>>>(L0.b, v, n);
   LAUNCHED();
-  int rc;
-  {
+  int rc = ATM_OK;
+  bool replayed = false;
+  if (mg.use_graphs && !H.graph_failed) {
+    const double key[4] = {implicit_coeff(c), c.dt, c.Ma, (double)H.lam_epoch};
+    if (!H.graph || std::memcmp(key, H.graph_key, sizeof(key)) != 0) {
+      if (capture_vcycle<T>(c, mg, H) == ATM_OK) {
+        std::memcpy(H.graph_key, key, sizeof(key));
+      } else {
+        H.graph_failed = true;  // keep running the V-cycle launch by launch
+        hier_drop_graph(H);
+      }
+    }
+    if (H.graph) {
+      TimedRegion tr(c, KF_MG_OTHER, 0.0, 0.0);  // whole V-cycle
+      ATM_CUDA(cudaGraphLaunch(H.graph, c.stream));
+      g_kernel_launches.fetch_add(H.graph_kernels);
+      ++mg.graph_replays;
+      replayed = true;
+    }
+  }
+  if (!replayed) {
     TimedRegion tr(c, KF_MG_OTHER, 0.0, 0.0);  // whole V-cycle (includes the level applies)
     rc = vcycle<T>(c, mg, H, 0);
   }
@@ -526,6 +608,7 @@ int mg_free(atm_ctx &c) {
   hier_free(c.mg->f);
   hier_free(c.mg->d);
   cudaFree(c.mg->zbasis);
+  if (c.mg->cap_stream) cudaStreamDestroy(c.mg->cap_stream);
   delete c.mg;
   c.mg = nullptr;
   return ATM_OK;
@@ -718,6 +801,8 @@ int mg_set_params(atm_ctx &c, int degree, double range, int eig_its, int coarse_
     set_error("atm_mg_set_smoother: bad parameters");
     return ATM_BAD_ARG;
   }
+  hier_drop_graph(c.mg->f);
+  hier_drop_graph(c.mg->d);
   c.mg->cheb_deg = degree;
   c.mg->range = range;
   c.mg->eig_its = eig_its;
@@ -727,6 +812,22 @@ int mg_set_params(atm_ctx &c, int degree, double range, int eig_its, int coarse_
 }
 
 long mg_vcycles(const atm_ctx &c) { return c.mg ? c.mg->vcycles : 0; }
+int mg_set_graphs(atm_ctx &c, bool on) {
+  if (!c.mg) {
+    set_error("atm_mg_set_graphs: add levels first");
+    return ATM_NOT_READY;
+  }
+  c.mg->use_graphs = on;
+  if (!on) {
+    hier_drop_graph(c.mg->f);
+    hier_drop_graph(c.mg->d);
+  }
+  return ATM_OK;
+}
+void mg_stats(const atm_ctx &c, long *out) {
+  out[0] = c.mg ? c.mg->vcycles : 0;
+  out[1] = c.mg ? c.mg->graph_replays : 0;
+}
 int mg_levels(const atm_ctx &c) { return c.mg ? (int)c.mg->hm.size() : 0; }
 
 }  // namespace atm

@@ -183,6 +183,15 @@ class EULEROperator:
         """One V-cycle, FP32 (precision 1) or FP64 (precision 2)."""
         _lib.call("atm_mg_vcycle", self._h, int(precision), _ptr(dst), _ptr(src))
 
+    def set_mg_graphs(self, on):
+        """Replay the V-cycle as a captured CUDA graph (default) or not."""
+        _lib.call("atm_mg_set_graphs", self._h, int(bool(on)))
+
+    def mg_stats(self):
+        out = (ctypes.c_long * 2)()
+        _lib.call("atm_mg_stats", self._h, out)
+        return {"vcycles": out[0], "graph_replays": out[1]}
+
     def set_true_residual_check(self, on):
         _lib.call("atm_set_true_residual_check", self._h, int(bool(on)))
 

@@ -192,6 +192,14 @@ int atm_mg_set_smoother(atm_handle h, int degree, double smoothing_range, int ei
 /* One V-cycle: dst ~= S^{-1} src (FP64 device vectors); precision 1 runs the
  * V-cycle in FP32, 2 in FP64. */
 int atm_mg_vcycle(atm_handle h, int precision, double *dst, const double *src);
+/* Replay the V-cycle as a captured CUDA graph (1, default) or launch its
+ * kernels one by one (0).  Same kernels, same arguments, same results; the
+ * graph is re-captured when the stage coefficient, dt, Ma or the smoother's
+ * eigenvalue estimates change.  No reference counterpart (deal.II's
+ * PreconditionMG::vmult, Atmospheric_Flow.cc:517-536, runs on the host). */
+int atm_mg_set_graphs(atm_handle h, int on);
+/* out[0] = V-cycles run, out[1] = of those, replays of a captured graph. */
+int atm_mg_stats(atm_handle h, long *out);
 /* FGMRES(16) + V-cycle on S x = b (NS 2 operator state); tol absolute on the
  * unpreconditioned residual; precision as for atm_mg_vcycle. */
 int atm_solve_fgmres(atm_handle h, int precision, double *x, const double *b, double tol,

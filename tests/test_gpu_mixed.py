@@ -114,3 +114,28 @@ def test_fp64_multigrid_steps_within_1e10_of_oracle(cuda_ok):
     for a, b, name in zip(g.get_state(), o.get_state(), ("rho", "u", "p")):
         err = np.linalg.norm(a - b) / np.linalg.norm(b)
         assert err < 1e-10, (name, err)
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+def test_vcycle_graph_replay_is_bitwise_the_launch_sequence(cuda_ok, precision):
+    """The captured-graph V-cycle equals the launch-by-launch one bit for bit,
+    and is re-captured when the stage coefficient or rho_fix changes."""
+    case = build_case(HillParams(nx=16, nz=8, degree=3, cfl=4.0))
+    op_g, rng = schur_op(case, seed=5)
+    op_e, _ = schur_op(case, seed=5)
+    op_e.set_mg_graphs(False)
+    b = dev(rng.standard_normal(op_g.n_scalar))
+    for stage, new_rho in ((1, False), (1, False), (2, False), (2, True)):
+        for op in (op_g, op_e):
+            op.set_HYPERBOLIC_stage(stage)
+            if new_rho:
+                op.set_rho_for_fixed(dev(case.rho * 1.001))
+        zg = torch.empty_like(b)
+        ze = torch.empty_like(b)
+        op_g.mg_vcycle(zg, b, precision)
+        op_e.mg_vcycle(ze, b, precision)
+        torch.cuda.synchronize()
+        assert torch.equal(zg, ze)
+    sg, se = op_g.mg_stats(), op_e.mg_stats()
+    assert sg["vcycles"] == se["vcycles"] == 4
+    assert sg["graph_replays"] == 4 and se["graph_replays"] == 0
