@@ -55,6 +55,8 @@ SIGNATURES = {
     "atm_mg_set_smoother": (_i, [_h, _i, _d, _i, _i]),
     "atm_mg_vcycle": (_i, [_h, _i, ctypes.c_void_p, ctypes.c_void_p]),
     "atm_mg_set_graphs": (_i, [_h, _i]),
+    "atm_set_autotune": (_i, [_h, _i]),
+    "atm_autotune_table": (_i, [ctypes.POINTER(ctypes.c_int), _i]),
     "atm_mg_stats": (_i, [_h, ctypes.POINTER(ctypes.c_long)]),
     "atm_solve_fgmres": (_i, [_h, _i, ctypes.c_void_p, ctypes.c_void_p, _d, _i, _ip, _dp]),
     "atm_set_true_residual_check": (_i, [_h, _i]),
@@ -111,3 +113,21 @@ def check(code: int, where: str) -> None:
 
 def call(name: str, *args) -> None:
     check(getattr(load(), name)(*args), name)
+
+
+TUNE_FAMILIES = ("rhs_rho", "rhs_vel", "rhs_pres", "B", "CD")
+
+
+def autotune_table():
+    """Cells-per-block choices of the autotuner so far (this process)."""
+    lib = load()
+    n = lib.atm_autotune_table(None, 0)
+    buf = (ctypes.c_int * (8 * max(n, 1)))()
+    n = lib.atm_autotune_table(buf, n)
+    rows = []
+    for i in range(n):
+        r = buf[8 * i: 8 * i + 8]
+        rows.append({"family": TUNE_FAMILIES[r[1]], "degree": r[2], "mode": r[3],
+                     "hanging": bool(r[4]), "bytes": r[5], "log2_cells": r[6],
+                     "cells_per_block": r[7]})
+    return rows

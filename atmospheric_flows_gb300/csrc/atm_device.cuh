@@ -24,8 +24,11 @@ struct Cfg {
   static constexpr int NQ = 2 * K + 1;
   static constexpr int NN2 = NN * NN;
   static constexpr int NQ2 = NQ * NQ;
-  static constexpr int CPB = 128 / NQ;  // cells per block
+  static constexpr int CPB = 128 / NQ;  // default cells per block
   static constexpr int THREADS = CPB * NQ;
+  // the face kernels take the cells per block from blockDim (autotuned among
+  // 64/NQ, 128/NQ and 256/NQ cells)
+  static constexpr int MAX_THREADS = (256 / NQ) * NQ;
 };
 
 // [degree][w][q*(k+1)+i]: w = 0 values and 1 derivatives at the 2k+1 Gauss
@@ -422,9 +425,9 @@ __device__ __forceinline__ QGeoT<T> qgeo(const T *__restrict__ g, int q) {
 
 // tiles, x-contraction exchange, face values [, subface-1 face values]
 template <int K, typename T = double>
-inline size_t smem_bytes(int n_tiles, int ncomp_out, bool hg = false) {
+inline size_t smem_bytes(int cpb, int n_tiles, int ncomp_out, bool hg = false) {
   using C = Cfg<K>;
-  return sizeof(T) * (size_t)C::CPB *
+  return sizeof(T) * (size_t)cpb *
          ((size_t)n_tiles * C::NN2 + (size_t)ncomp_out * 2 * C::NN * C::NQ +
           (size_t)ncomp_out * 4 * C::NQ * (hg ? 2 : 1));
 }

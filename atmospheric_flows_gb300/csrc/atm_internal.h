@@ -5,6 +5,7 @@
 #include <atomic>
 #include <cstdint>
 #include <string>
+#include <functional>
 #include <vector>
 
 #include "../../include/atm_gb300.h"
@@ -106,6 +107,7 @@ struct atm_ctx {
   atm::MG *mg = nullptr;  // multigrid hierarchy of the FGMRES Schur solves
   // GMRES/FGMRES only stop on a recomputed true residual (S is nonlinear)
   bool true_residual_check = false;
+  bool autotune = true;  // choose the face kernels' cells per block by timing
   mutable atm::KTimer timer;
   bool capturing = false;  // a CUDA graph is being recorded: timers are off
   long n_scalar() const { return (long)nc * nn2; }
@@ -218,6 +220,7 @@ struct LevelViewT {
   const T *ainv;  // [nc][nn2*nn2] inverse rho_fix-weighted mass (transposed)
   const T *invd;  // inverse diagonal of D
   cudaStream_t st;
+  bool tune = false;  // the autotuner may time tile shapes on this stream
 };
 template <typename T>
 int level_B(const LevelViewT<T> &v, T *dst, const T *p, T cB, int mode);
@@ -240,6 +243,20 @@ int fgmres_mg(atm_ctx &c, int precision, double *x, const double *b, double tol,
               int *its, double *res);
 void mg_mark_rho_changed(atm_ctx &c);
 long mg_vcycles(const atm_ctx &c);
+
+// ------------------------------------------------------------- autotuner --
+// Cells per block of the face kernels, among 64/NQ, 128/NQ and 256/NQ, per
+// (device, kernel family, degree, mode or stage, hanging faces, value size,
+// log2 of the cell count).  On the first idempotent launch of a key with
+// tuning allowed, `launch(cpb)` is timed for each candidate (1 warm-up + 3
+// timed launches, CUDA events on `st`) and the fastest is kept; until then,
+// for meshes below 2048 cells, and when tuning is off the default 128/NQ is
+// used.  The choice never changes results: every cell is computed by its own
+// threads whatever the block grouping.
+enum TuneFamily { TF_RHS_RHO = 0, TF_RHS_VEL, TF_RHS_PRES, TF_B, TF_CD };
+int tuned_cpb(bool tune, cudaStream_t st, int family, int k, int mode, bool hg, int tsize,
+              int nc, bool idempotent, const std::function<cudaError_t(int)> &launch);
+int tune_table(int *out, int max_entries);
 int mg_set_graphs(atm_ctx &c, bool on);
 void mg_stats(const atm_ctx &c, long *out);
 int mg_levels(const atm_ctx &c);

@@ -366,6 +366,18 @@ int atm_mg_vcycle(atm_handle h, int precision, double *dst, const double *src) {
   if (precision != 1 && precision != 2) { set_error("precision must be 1 or 2"); return ATM_BAD_ARG; }
   return mg_precondition(*h, precision, dst, src);
 }
+int atm_set_autotune(atm_handle h, int on) {
+  CHECK_H(h);
+  h->autotune = on != 0;
+  return ATM_OK;
+}
+int atm_autotune_table(int *out, int max_entries) {
+  if (max_entries < 0) {
+    set_error("atm_autotune_table: max_entries < 0");
+    return ATM_BAD_ARG;
+  }
+  return tune_table(out, max_entries);
+}
 int atm_mg_set_graphs(atm_handle h, int on) {
   CHECK_H(h);
   return mg_set_graphs(*h, on != 0);

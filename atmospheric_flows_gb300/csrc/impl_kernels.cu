@@ -388,23 +388,23 @@ int launch_block_apply(const atm_ctx &c, double *dst, const double *src, const d
 // ---- launchers on a multigrid level (untimed; float or double) -----------
 template <typename T>
 int level_B(const LevelViewT<T> &v, T *dst, const T *p, T cB, int mode) {
-  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st};
+  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune};
   ATM_DISPATCH_K(v.k, (B_launch<K, T, false>(o, dst, p, cB, mode)));
 }
 template <typename T>
 int level_CD(const LevelViewT<T> &v, T *dst, const T *w, const T *p, const T *pfix, T cC,
              int mode) {
-  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st};
+  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune};
   ATM_DISPATCH_K(v.k, (CD_launch<K, T, false>(o, dst, w, p, pfix, cC, mode)));
 }
 template <typename T>
 int level_inv_diag(const LevelViewT<T> &v, T *out, T scale) {
-  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st};
+  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune};
   ATM_DISPATCH_K(v.k, (invdiag_launch<K, T>(o, out, 1, (const T *)nullptr, scale)));
 }
 template <typename T>
 int level_block_inverse(const LevelViewT<T> &v, T *out, const T *weight) {
-  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st};
+  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune};
   ATM_DISPATCH_K(v.k, (block_inverse_launch<K, T>(o, out, weight)));
 }
 #define ATM_LEVEL_INST(T)                                                                   \

@@ -252,7 +252,7 @@ inline int gsz(long n) {
 
 template <typename T>
 LevelViewT<T> lview(const atm_ctx &c, const MGLevelT<T> &L) {
-  return LevelViewT<T>{c.k, L.nc, L.mesh, L.ainv, L.invd, c.stream};
+  return LevelViewT<T>{c.k, L.nc, L.mesh, L.ainv, L.invd, c.stream, c.autotune && !c.capturing};
 }
 
 template <typename T>

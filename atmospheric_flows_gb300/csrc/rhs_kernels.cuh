@@ -22,10 +22,11 @@ namespace atm {
 
 // ============================================================== rho rhs ===
 template <int K, int ST, bool HG>
-__global__ void __launch_bounds__(Cfg<K>::THREADS)
+__global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     k_rhs_rho(double *__restrict__ dst, SrcPtrs src, StageCoef co, Mesh mesh) {
   using C = Cfg<K>;
-  constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2, CPB = C::CPB;
+  constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2;
+  const int CPB = blockDim.x / NQ;  // cells per block, chosen by the autotuner
   constexpr int NT = 3 * ST;
   extern __shared__ double sm[];
   double *tiles = sm;
@@ -113,10 +114,11 @@ __global__ void __launch_bounds__(Cfg<K>::THREADS)
 
 // ========================================================= momentum rhs ===
 template <int K, int ST, bool HG>
-__global__ void __launch_bounds__(Cfg<K>::THREADS)
+__global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     k_rhs_vel(double *__restrict__ dst, SrcPtrs src, StageCoef co, Mesh mesh) {
   using C = Cfg<K>;
-  constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2, CPB = C::CPB;
+  constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2;
+  const int CPB = blockDim.x / NQ;  // cells per block, chosen by the autotuner
   constexpr int NG = (ST == 1) ? 2 : 3;             // gravity terms
   constexpr int NT = 4 * ST + (ST < 3 ? 1 : 0);     // tiles
   extern __shared__ double sm[];
@@ -255,10 +257,11 @@ __global__ void __launch_bounds__(Cfg<K>::THREADS)
 
 // ======================================================== energy rhs (p) ===
 template <int K, int ST, bool HG>
-__global__ void __launch_bounds__(Cfg<K>::THREADS)
+__global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     k_rhs_pres(double *__restrict__ dst, SrcPtrs src, StageCoef co, Mesh mesh) {
   using C = Cfg<K>;
-  constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2, CPB = C::CPB;
+  constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2;
+  const int CPB = blockDim.x / NQ;  // cells per block, chosen by the autotuner
   constexpr int NG = (ST == 1) ? 2 : 3;
   constexpr int NT = 4 * ST + 3;
   constexpr double GM1 = GAS_GAMMA - 1.0;
@@ -408,20 +411,32 @@ int rhs_launch(const atm_ctx &c, int kind, int stage, double *dst, const double 
   const int nsrc_tab[3][3] = {{2, 4, 6}, {4, 7, 9}, {5, 8, 11}};
   const int nsrc = nsrc_tab[kind][stage - 1];
   for (int i = 0; i < nsrc; ++i) sp.p[i] = src[i];
-  const int grid = (c.nc + C::CPB - 1) / C::CPB;
-  size_t sm;
+  int ntile;
   void (*fn)(double *, SrcPtrs, StageCoef, Mesh) = nullptr;
   if (kind == 0) {
-    sm = smem_bytes<K>(3 * stage, 1, HG);
+    ntile = 3 * stage;
     fn = stage == 1 ? k_rhs_rho<K, 1, HG> : (stage == 2 ? k_rhs_rho<K, 2, HG> : k_rhs_rho<K, 3, HG>);
   } else if (kind == 1) {
-    sm = smem_bytes<K>(4 * stage + (stage < 3 ? 1 : 0), 2, HG);
+    ntile = 4 * stage + (stage < 3 ? 1 : 0);
     fn = stage == 1 ? k_rhs_vel<K, 1, HG> : (stage == 2 ? k_rhs_vel<K, 2, HG> : k_rhs_vel<K, 3, HG>);
   } else {
-    sm = smem_bytes<K>(4 * stage + 3, 1, HG);
+    ntile = 4 * stage + 3;
     fn = stage == 1 ? k_rhs_pres<K, 1, HG> : (stage == 2 ? k_rhs_pres<K, 2, HG> : k_rhs_pres<K, 3, HG>);
   }
-  if (sm > 48 * 1024) ATM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  const int ncomp = kind == 1 ? 2 : 1;
+  auto launch = [&](int cpb) -> cudaError_t {
+    const size_t sm = smem_bytes<K>(cpb, ntile, ncomp, HG);
+    if (sm > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return e;
+    }
+    fn<<<(c.nc + cpb - 1) / cpb, cpb * C::NQ, sm, c.stream>>>(dst, sp, co, c.mesh);
+    return cudaGetLastError();
+  };
+  bool idem = true;  // the kernel only writes dst: safe to run repeatedly
+  for (int i = 0; i < nsrc; ++i) idem = idem && src[i] != dst;
+  const int cpb = tuned_cpb(c.autotune && !c.capturing, c.stream, TF_RHS_RHO + kind, K, stage,
+                            HG, 8, c.nc, idem, launch);
   // algorithmic bytes: every source field read once, the result written once
   const double ns = (double)c.nc * C::NN2;
   const int nfields = (kind == 0) ? 3 * stage : (kind == 1 ? 4 * stage + (stage < 3) : 4 * stage + 3);
@@ -433,8 +448,8 @@ int rhs_launch(const atm_ctx &c, int kind, int stage, double *dst, const double 
   const double flops = c.nc * (nfields * fl_eval(K) + nout * fl_integrate(K, true) +
                                4.0 * (2 * ntrace * fl_face(K) + nout * fl_face(K)));
   TimedRegion tr(c, KF_RHS_RHO + kind, bytes, flops);
-  fn<<<grid, C::THREADS, sm, c.stream>>>(dst, sp, co, c.mesh);
-  ATM_CHECK_LAUNCH("rhs kernel");
+  ATM_CUDA(launch(cpb));
+  g_kernel_launches.fetch_add(1);
   return ATM_OK;
 }
 

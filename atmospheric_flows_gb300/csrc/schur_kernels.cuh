@@ -14,11 +14,12 @@ namespace atm {
 // ====================================================================== B ===
 // MODE 0: dst = B p ; 1: dst -= B p ; 2: dst = A^{-1} B p
 template <int K, int MODE, typename T, bool HG>
-__global__ void __launch_bounds__(Cfg<K>::THREADS)
+__global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     k_B(T *__restrict__ dst, const T *__restrict__ p, T cB,
         const T *__restrict__ ainv, MeshT<T> mesh) {
   using C = Cfg<K>;
-  constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2, CPB = C::CPB;
+  constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2;
+  const int CPB = blockDim.x / NQ;  // cells per block, chosen by the autotuner
   constexpr int NT = 1;
   extern __shared__ __align__(16) unsigned char sm_raw[];
   T *sm = reinterpret_cast<T *>(sm_raw);
@@ -119,12 +120,13 @@ __global__ void __launch_bounds__(Cfg<K>::THREADS)
 // MODE 0: dst = C w ; 1: dst = sD D p - C w ; 2: dst = invd .* (sD D p - C w)
 // MODE 3: dst -= C w
 template <int K, int MODE, typename T, bool HG>
-__global__ void __launch_bounds__(Cfg<K>::THREADS)
+__global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     k_CD(T *__restrict__ dst, const T *__restrict__ w, const T *__restrict__ p,
          const T *__restrict__ pfix, T cC, const T *__restrict__ invd,
          MeshT<T> mesh) {
   using C = Cfg<K>;
-  constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2, CPB = C::CPB;
+  constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2;
+  const int CPB = blockDim.x / NQ;  // cells per block, chosen by the autotuner
   constexpr bool WITH_D = (MODE == 1 || MODE == 2);
   constexpr int NT = WITH_D ? 4 : 3;  // w(2), pfix, [p]
   constexpr T GM1 = GAS_GAMMA - T(1.0);
@@ -214,21 +216,34 @@ struct OpView {
   const T *ainv;
   const T *invd;
   cudaStream_t st;
+  bool tune;  // the autotuner may time tile shapes on this stream
 };
 
 inline OpView<double> schur_view(const atm_ctx &c) {
-  return OpView<double>{c.k, c.nc, c.mesh, c.ainv, c.invdiag_D, c.stream};
+  return OpView<double>{c.k, c.nc, c.mesh, c.ainv, c.invdiag_D, c.stream,
+                        c.autotune && !c.capturing};
 }
 
 template <int K, typename T, bool HG>
 int B_launch(const OpView<T> &v, T *dst, const T *p, T cB, int mode) {
   using C = Cfg<K>;
-  const int grid = (v.nc + C::CPB - 1) / C::CPB;
-  const size_t sm = smem_bytes<K, T>(1, 2, HG) + sizeof(T) * C::CPB * 2 * C::NN2;
-  if (mode == 0) k_B<K, 0, T, HG><<<grid, C::THREADS, sm, v.st>>>(dst, p, cB, v.ainv, v.mesh);
-  else if (mode == 1) k_B<K, 1, T, HG><<<grid, C::THREADS, sm, v.st>>>(dst, p, cB, v.ainv, v.mesh);
-  else k_B<K, 2, T, HG><<<grid, C::THREADS, sm, v.st>>>(dst, p, cB, v.ainv, v.mesh);
-  ATM_CHECK_LAUNCH("k_B");
+  auto launch = [&](int cpb) -> cudaError_t {
+    const int grid = (v.nc + cpb - 1) / cpb, th = cpb * C::NQ;
+    const size_t sm = smem_bytes<K, T>(cpb, 1, 2, HG) + sizeof(T) * cpb * 2 * C::NN2;
+    void (*fn)(T *, const T *, T, const T *, MeshT<T>) =
+        mode == 0 ? k_B<K, 0, T, HG> : (mode == 1 ? k_B<K, 1, T, HG> : k_B<K, 2, T, HG>);
+    if (sm > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return e;
+    }
+    fn<<<grid, th, sm, v.st>>>(dst, p, cB, v.ainv, v.mesh);
+    return cudaGetLastError();
+  };
+  // mode 1 (dst -= B p) is not idempotent: it uses the choice made for mode 0
+  const int cpb = tuned_cpb(v.tune, v.st, TF_B, K, mode == 1 ? 0 : mode, HG, (int)sizeof(T),
+                            v.nc, mode != 1 && dst != p, launch);
+  ATM_CUDA(launch(cpb));
+  g_kernel_launches.fetch_add(1);
   return ATM_OK;
 }
 
@@ -236,18 +251,27 @@ template <int K, typename T, bool HG>
 int CD_launch(const OpView<T> &v, T *dst, const T *w, const T *p, const T *pfix, T cC,
               int mode) {
   using C = Cfg<K>;
-  const int grid = (v.nc + C::CPB - 1) / C::CPB;
-  const size_t sm = smem_bytes<K, T>(4, 1, HG);
-  switch (mode) {
-    case 0: k_CD<K, 0, T, HG><<<grid, C::THREADS, sm, v.st>>>(dst, w, p, pfix, cC, v.invd, v.mesh); break;
-    case 1: k_CD<K, 1, T, HG><<<grid, C::THREADS, sm, v.st>>>(dst, w, p, pfix, cC, v.invd, v.mesh); break;
-    case 2: k_CD<K, 2, T, HG><<<grid, C::THREADS, sm, v.st>>>(dst, w, p, pfix, cC, v.invd, v.mesh); break;
-    default: k_CD<K, 3, T, HG><<<grid, C::THREADS, sm, v.st>>>(dst, w, p, pfix, cC, v.invd, v.mesh); break;
-  }
-  ATM_CHECK_LAUNCH("k_CD");
+  auto launch = [&](int cpb) -> cudaError_t {
+    const int grid = (v.nc + cpb - 1) / cpb, th = cpb * C::NQ;
+    const size_t sm = smem_bytes<K, T>(cpb, 4, 1, HG);
+    void (*fn)(T *, const T *, const T *, const T *, T, const T *, MeshT<T>) =
+        mode == 0 ? k_CD<K, 0, T, HG>
+                  : (mode == 1 ? k_CD<K, 1, T, HG> : (mode == 2 ? k_CD<K, 2, T, HG> : k_CD<K, 3, T, HG>));
+    if (sm > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return e;
+    }
+    fn<<<grid, th, sm, v.st>>>(dst, w, p, pfix, cC, v.invd, v.mesh);
+    return cudaGetLastError();
+  };
+  // mode 3 (dst -= C w) is not idempotent: it uses the choice made for mode 0
+  const bool idem = mode != 3 && dst != w && dst != p && dst != pfix;
+  const int cpb = tuned_cpb(v.tune, v.st, TF_CD, K, mode == 3 ? 0 : mode, HG, (int)sizeof(T),
+                            v.nc, idem, launch);
+  ATM_CUDA(launch(cpb));
+  g_kernel_launches.fetch_add(1);
   return ATM_OK;
 }
-
 
 #define ATM_DISPATCH_K(kk, call)          \
   switch (kk) {                           \

@@ -80,7 +80,12 @@ extern "C" int atm_schur_vmult_static_scratch(atm_handle h, double *dst, const d
   int rc = scratch_address(dev, &scratch);
   if (rc) return rc;
   const double co = implicit_coeff(*h);
+  // no tile-shape timing here (it would create events): tuned choices made by
+  // earlier calls are used, otherwise the default blocks
+  const bool tune = h->autotune;
+  h->autotune = false;
   rc = launch_B(*h, scratch, src, co * h->dt / (h->Ma * h->Ma), 2);
-  if (rc) return rc;
-  return launch_CD(*h, dst, scratch, src, h->pres_fix, co * h->dt, 1);
+  if (rc == ATM_OK) rc = launch_CD(*h, dst, scratch, src, h->pres_fix, co * h->dt, 1);
+  h->autotune = tune;
+  return rc;
 }

@@ -200,6 +200,19 @@ int atm_mg_vcycle(atm_handle h, int precision, double *dst, const double *src);
 int atm_mg_set_graphs(atm_handle h, int on);
 /* out[0] = V-cycles run, out[1] = of those, replays of a captured graph. */
 int atm_mg_stats(atm_handle h, long *out);
+
+/* Tile-shape autotuner of the face kernels (the explicit right-hand sides, B
+ * and C/D, on every level): cells per block among 64/(2k+1), 128/(2k+1) and
+ * 256/(2k+1), timed on the first launch of each (kernel, degree, mode, mesh
+ * size class) on meshes of 2048 cells or more.  On by default; results do not
+ * depend on it.  No reference counterpart (deal.II's MatrixFree fixes its
+ * cell batch size at compile time, Atmospheric_Flow.cc:337-344). */
+int atm_set_autotune(atm_handle h, int on);
+/* The choices made so far in this process: up to max_entries rows of 8 ints
+ * (device, family 0 rhs_rho / 1 rhs_vel / 2 rhs_pres / 3 B / 4 C/D, degree,
+ * mode or stage, hanging faces, bytes per value, log2 of the cell count,
+ * cells per block).  Returns the number of entries (may exceed max_entries). */
+int atm_autotune_table(int *out, int max_entries);
 /* FGMRES(16) + V-cycle on S x = b (NS 2 operator state); tol absolute on the
  * unpreconditioned residual; precision as for atm_mg_vcycle. */
 int atm_solve_fgmres(atm_handle h, int precision, double *x, const double *b, double tol,
