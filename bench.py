@@ -380,6 +380,10 @@ def run_gb300(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": workload(args), "e2e": e2e,
             "gpu_launches": int(main["launches"]), "roofline": roofline, "cpu_baseline": cpu,
+            "autotune": [{k: r[k] for k in ("family", "mode", "cells_per_block")}
+                         for r in _lib.autotune_table()
+                         if r["degree"] == args.degree and r["bytes"] == 8 and not r["hanging"]
+                         and r["log2_cells"] == int(np.log2(case.n_cells))],
             "clocks": clk.summary(),
             "solver": {"scheme": "the reference's Schur solver on the GPU: GMRES(28) + Jacobi on "
                                  "diag(D), eps 1e-8 (parameter-file.prm) on the Jacobi-scaled "
