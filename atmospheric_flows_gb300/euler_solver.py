@@ -28,8 +28,13 @@ class EulerSolver:
     PRECISION_MIXED = 1   # FGMRES + FP32 multigrid V-cycle
     PRECISION_FP64_MG = 2  # FGMRES + FP64 multigrid V-cycle
 
-    def __init__(self, case, eps=1e-8, max_its=30000, precision=0, dt=None, mg_levels=8,
+    def __init__(self, case, eps=1e-8, max_its=None, precision=0, dt=None, mg_levels=8,
                  true_residual_check=False, stream=None):
+        # Krylov iteration cap per Schur solve: the reference's GMRES cap for
+        # precision 0; multigrid-preconditioned FGMRES needs tens, so a solve
+        # that stalls gives up after 1000 instead of running for minutes
+        if max_its is None:
+            max_its = 30000 if int(precision) == 0 else 1000
         self.case = case
         self.op = EULEROperator(MatrixFreeStorage.from_case(case))
         self.stream = stream
