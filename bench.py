@@ -162,9 +162,10 @@ def measured_peaks():
 # independent-chain DFMA probe; profiles/fp64_fp32_fma_peak.md)
 FP64_PEAK_TFLOPS = 1.255
 # DRAM bytes (read + write) per cell and launch of the dominant kernel families,
-# from `ncu` captures of this bench at 320x160 (profiles/k_CD_q4_320x160.md);
+# from `ncu` captures of this bench at 320x160 (profiles/k_CD_q4_320x160.md,
+# profiles/k_B_q4_320x160.md);
 # the traffic grows in proportion to the cell count.
-NCU_TRAFFIC_PER_CELL = {4: {"CD": 273.1e6 / 51200}}
+NCU_TRAFFIC_PER_CELL = {4: {"CD": 273.1e6 / 51200, "B": 469.6e6 / 51200}}
 
 
 def cpu_baseline(case, eps):
