@@ -224,6 +224,85 @@ __device__ __forceinline__ void integrate_col_z(const T (&V)[2 * K + 1], const T
   }
 }
 
+// Output phase by rows (conforming meshes), thread t < k+1 owns row iz = t:
+//   out[ix] = sum_qx S(qx,ix) r[qx] + D(qx,ix) xb[iz][qx]
+//           + [ix = 0] sum_q S(q,iz) F0[q] + [ix = k] sum_q S(q,iz) F1[q]
+// with r = xa[iz] plus the z-face values (F2 on row 0, F3 on row k: the face
+// points of z-faces are the x quadrature points, so those terms fold into the
+// same contraction).  The x-contraction uses the even-odd split over the
+// point pairs (qx, 2k-qx), as integrate_col_z.  St holds S(., iz); F is the
+// cell's [4][NQ] face values of this component.
+template <int K, typename T>
+__device__ __forceinline__ void integrate_row(const T *__restrict__ xa, const T *__restrict__ xb,
+                                              const T *__restrict__ F, int iz,
+                                              const T (&St)[2 * K + 1], T (&out)[K + 1]) {
+  constexpr int NQ = 2 * K + 1, H = (K + 1) / 2;
+  constexpr bool MID = ((K + 1) & 1) != 0;
+  T r[NQ], g[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    T v = xa[iz * NQ + q];
+    if (iz == 0) v += F[2 * NQ + q];
+    if (iz == K) v += F[3 * NQ + q];
+    r[q] = v;
+    g[q] = xb[iz * NQ + q];
+  }
+  T re[K], ro[K], ge[K], go[K];
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+    re[q] = r[q] + r[NQ - 1 - q];
+    ro[q] = r[q] - r[NQ - 1 - q];
+    ge[q] = g[q] + g[NQ - 1 - q];
+    go[q] = g[q] - g[NQ - 1 - q];
+  }
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    T e = bS<K, T>(K, i) * r[K], o = bD<K, T>(K, i) * g[K];
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      e = fma(bEO<K, T>(4, q, i), re[q], e);
+      e = fma(bEO<K, T>(6, q, i), go[q], e);
+      o = fma(bEO<K, T>(5, q, i), ro[q], o);
+      o = fma(bEO<K, T>(7, q, i), ge[q], o);
+    }
+    out[i] = e + o;
+    out[K - i] = e - o;
+  }
+  if (MID) {
+    T e = bS<K, T>(K, H) * r[K];
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      e = fma(bS<K, T>(q, H), re[q], e);
+      e = fma(bD<K, T>(q, H), go[q], e);
+    }
+    out[H] = e;
+  }
+  T s0 = 0, s1 = 0;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    s0 = fma(St[q], F[q], s0);
+    s1 = fma(St[q], F[NQ + q], s1);
+  }
+  out[0] += s0;
+  out[K] += s1;
+}
+
+// local node written by output slot j of thread t: column layout (hanging-
+// face kernels: node (iz = j, ix = t)) or row layout (node (iz = t, ix = j))
+template <int K, bool HG>
+__device__ __forceinline__ int out_node(int t, int j) {
+  return HG ? j * (K + 1) + t : t * (K + 1) + j;
+}
+
+// output phase of one component: rows (conforming) or columns + face terms
+// (hanging faces, add_face_out_hg)
+template <int K, bool HG, typename T>
+__device__ __forceinline__ void output_phase(const MeshT<T> &mesh, int c, const T *__restrict__ xa,
+                                             const T *__restrict__ xb, const T *__restrict__ F,
+                                             const T *__restrict__ Fh, int t,
+                                             const T (&St)[2 * K + 1], const T (&Dt)[2 * K + 1],
+                                             T (&out)[K + 1]);
+
 // x-contraction for output node column ix = t: out[iz] = sum_qx S(qx,t) xa + D(qx,t) xb
 template <int K, bool HAS_G, typename T>
 __device__ __forceinline__ void integrate_out(const T *__restrict__ xa, const T *__restrict__ xb,
@@ -376,6 +455,20 @@ __device__ __forceinline__ void add_faces(const MeshT<T> &mesh, int c, const T *
                                           const T (&St)[2 * K + 1], T (&out)[K + 1]) {
   if (HG) add_face_out_hg<K>(F, Fh, hanging_mask(mesh, c), t, St, out);
   else add_face_out<K>(F, t, St, out);
+}
+
+template <int K, bool HG, typename T>
+__device__ __forceinline__ void output_phase(const MeshT<T> &mesh, int c, const T *__restrict__ xa,
+                                             const T *__restrict__ xb, const T *__restrict__ F,
+                                             const T *__restrict__ Fh, int t,
+                                             const T (&St)[2 * K + 1], const T (&Dt)[2 * K + 1],
+                                             T (&out)[K + 1]) {
+  if (HG) {
+    integrate_out<K, true>(xa, xb, St, Dt, out);
+    add_face_out_hg<K>(F, Fh, hanging_mask(mesh, c), t, St, out);
+  } else {
+    integrate_row<K>(xa, xb, F, t, St, out);
+  }
 }
 
 // trace of a nodal tile at face quadrature point `col` (row Sx = S[col][.])

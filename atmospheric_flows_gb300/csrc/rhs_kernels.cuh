@@ -104,11 +104,11 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     double St[NQ], Dt[NQ], out[NN];
     load_cols<K>(col, St, Dt);
     const double *xa = xab + lc * 2 * NN * NQ;
-    integrate_out<K, true>(xa, xa + NN * NQ, St, Dt, out);
-    add_faces<K, HG>(mesh, c, fb + lc * 4 * NQ, fh + lc * 4 * NQ, col, St, out);
+    output_phase<K, HG>(mesh, c, xa, xa + NN * NQ, fb + lc * 4 * NQ, fh + lc * 4 * NQ, col, St, Dt,
+                        out);
     double *d = dst + (long)c * NN2;
 #pragma unroll
-    for (int iz = 0; iz < NN; ++iz) d[iz * NN + col] = out[iz];
+    for (int iz = 0; iz < NN; ++iz) d[out_node<K, HG>(col, iz)] = out[iz];
   }
 }
 
@@ -245,12 +245,11 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     for (int comp = 0; comp < 2; ++comp) {
       double out[NN];
       const double *xa = xab + (lc * 2 + comp) * 2 * NN * NQ;
-      integrate_out<K, true>(xa, xa + NN * NQ, St, Dt, out);
-      add_faces<K, HG>(mesh, c, fb + (lc * 2 + comp) * 4 * NQ, fh + (lc * 2 + comp) * 4 * NQ, col, St,
-                       out);
+      output_phase<K, HG>(mesh, c, xa, xa + NN * NQ, fb + (lc * 2 + comp) * 4 * NQ, fh + (lc * 2 + comp) * 4 * NQ, col, St, Dt,
+                          out);
       double *d = dst + ((long)c * 2 + comp) * NN2;
 #pragma unroll
-      for (int iz = 0; iz < NN; ++iz) d[iz * NN + col] = out[iz];
+      for (int iz = 0; iz < NN; ++iz) d[out_node<K, HG>(col, iz)] = out[iz];
     }
   }
 }
@@ -394,11 +393,11 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     double St[NQ], Dt[NQ], out[NN];
     load_cols<K>(col, St, Dt);
     const double *xa = xab + lc * 2 * NN * NQ;
-    integrate_out<K, true>(xa, xa + NN * NQ, St, Dt, out);
-    add_faces<K, HG>(mesh, c, fb + lc * 4 * NQ, fh + lc * 4 * NQ, col, St, out);
+    output_phase<K, HG>(mesh, c, xa, xa + NN * NQ, fb + lc * 4 * NQ, fh + lc * 4 * NQ, col, St, Dt,
+                        out);
     double *d = dst + (long)c * NN2;
 #pragma unroll
-    for (int iz = 0; iz < NN; ++iz) d[iz * NN + col] = out[iz];
+    for (int iz = 0; iz < NN; ++iz) d[out_node<K, HG>(col, iz)] = out[iz];
   }
 }
 

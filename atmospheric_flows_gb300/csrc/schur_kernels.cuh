@@ -80,18 +80,17 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     for (int comp = 0; comp < 2; ++comp) {
       T out[NN];
       const T *xa = xab + (lc * 2 + comp) * 2 * NN * NQ;
-      integrate_out<K, true>(xa, xa + NN * NQ, St, Dt, out);
-      add_faces<K, HG>(mesh, c, fb + (lc * 2 + comp) * 4 * NQ, fh + (lc * 2 + comp) * 4 * NQ,
-                       col, St, out);
+      output_phase<K, HG>(mesh, c, xa, xa + NN * NQ, fb + (lc * 2 + comp) * 4 * NQ, fh + (lc * 2 + comp) * 4 * NQ, col, St, Dt,
+                          out);
       if (MODE == 2) {
 #pragma unroll
-        for (int iz = 0; iz < NN; ++iz) bt[(lc * 2 + comp) * NN2 + iz * NN + col] = out[iz];
+        for (int iz = 0; iz < NN; ++iz) bt[(lc * 2 + comp) * NN2 + out_node<K, HG>(col, iz)] = out[iz];
       } else {
         T *d = dst + ((long)c * 2 + comp) * NN2;
 #pragma unroll
         for (int iz = 0; iz < NN; ++iz) {
-          if (MODE == 0) d[iz * NN + col] = out[iz];
-          else d[iz * NN + col] -= out[iz];
+          if (MODE == 0) d[out_node<K, HG>(col, iz)] = out[iz];
+          else d[out_node<K, HG>(col, iz)] -= out[iz];
         }
       }
     }
@@ -195,12 +194,12 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     T St[NQ], Dt[NQ], out[NN];
     load_cols<K>(col, St, Dt);
     const T *xa = xab + lc * 2 * NN * NQ;
-    integrate_out<K, true>(xa, xa + NN * NQ, St, Dt, out);
-    add_faces<K, HG>(mesh, c, fb + lc * 4 * NQ, fh + lc * 4 * NQ, col, St, out);
+    output_phase<K, HG>(mesh, c, xa, xa + NN * NQ, fb + lc * 4 * NQ, fh + lc * 4 * NQ, col, St, Dt,
+                        out);
     T *d = dst + (long)c * NN2;
 #pragma unroll
     for (int iz = 0; iz < NN; ++iz) {
-      const int i = iz * NN + col;
+      const int i = out_node<K, HG>(col, iz);
       if (MODE == 2) d[i] = invd[(long)c * NN2 + i] * out[iz];
       else if (MODE == 3) d[i] -= out[iz];
       else d[i] = out[iz];
