@@ -91,6 +91,7 @@ struct atm_ctx {
   atm::Tableau tab;
   // frozen fields (owned copies) and derived data
   double *rho_fix = nullptr, *pres_fix = nullptr, *u_fix = nullptr;
+  double *pfq = nullptr, *pff = nullptr;  // p_fix at quadrature points / face traces
   double *ainv = nullptr;       // [nc][nn2*nn2] inverse of rho_fix-weighted mass
   double *invdiag_D = nullptr;  // inverse diagonal of D (Schur Jacobi)
   // workspace
@@ -169,8 +170,12 @@ int launch_B(const atm_ctx &c, double *dst, const double *p, double coeff, int m
 //   mode 1: dst = sD*D p - C w
 //   mode 2: dst = invdiag .* (sD*D p - C w)
 //   mode 3: dst -= C w
-int launch_CD(const atm_ctx &c, double *dst, const double *w, const double *p,
-              const double *pfix, double coeff, int mode);
+// (C uses the context's frozen p_fix, prepared by launch_pfix_prep)
+int launch_CD(const atm_ctx &c, double *dst, const double *w, const double *p, double coeff,
+              int mode);
+// values of p_fix at the quadrature points and its face traces (after every
+// change of p_fix)
+int launch_pfix_prep(const atm_ctx &c);
 // matrix-free mass apply: dst = M_w src, weight = tile field or constant scale
 int launch_mass(const atm_ctx &c, double *dst, const double *src, int ncomp,
                 const double *weight, double scale);
@@ -221,12 +226,14 @@ struct LevelViewT {
   const T *invd;  // inverse diagonal of D
   cudaStream_t st;
   bool tune = false;  // the autotuner may time tile shapes on this stream
+  const T *pfix = nullptr, *pfq = nullptr, *pff = nullptr;  // level p_fix (+ prepared)
 };
 template <typename T>
 int level_B(const LevelViewT<T> &v, T *dst, const T *p, T cB, int mode);
 template <typename T>
-int level_CD(const LevelViewT<T> &v, T *dst, const T *w, const T *p, const T *pfix, T cC,
-             int mode);
+int level_CD(const LevelViewT<T> &v, T *dst, const T *w, const T *p, T cC, int mode);
+template <typename T>
+int level_pfix_prep(const LevelViewT<T> &v);
 template <typename T>
 int level_inv_diag(const LevelViewT<T> &v, T *out, T scale);
 template <typename T>

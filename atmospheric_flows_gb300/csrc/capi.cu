@@ -75,6 +75,8 @@ static void ctx_free(atm_ctx *c) {
   mesh_free(c->mesh);
   cudaFree(c->rho_fix);
   cudaFree(c->pres_fix);
+  cudaFree(c->pfq);
+  cudaFree(c->pff);
   cudaFree(c->u_fix);
   cudaFree(c->ainv);
   cudaFree(c->invdiag_D);
@@ -124,6 +126,8 @@ int atm_ctx_create(int dim, int degree, int n_cells, int mapping_degree,
   } while (0)
   ALLOC(c->rho_fix, ns);
   ALLOC(c->pres_fix, ns);
+  ALLOC(c->pfq, (long)n_cells * c->nq2);
+  ALLOC(c->pff, (long)n_cells * 4 * c->nq);
   ALLOC(c->u_fix, nv);
   ALLOC(c->ainv, blk);
   ALLOC(c->invdiag_D, ns);
@@ -267,7 +271,8 @@ int atm_set_rho_for_fixed(atm_handle h, const double *rho) {
 int atm_set_pres_fixed(atm_handle h, const double *p) {
   CHECK_H(h);
   CHECK_PTR(p, "pres");
-  return vec_copy(h->stream, h->pres_fix, p, h->n_scalar());
+  int rc = vec_copy(h->stream, h->pres_fix, p, h->n_scalar());
+  return rc ? rc : launch_pfix_prep(*h);
 }
 int atm_set_u_fixed(atm_handle h, const double *u) {
   CHECK_H(h);
@@ -318,7 +323,7 @@ int atm_vmult_enthalpy(atm_handle h, double *dst, const double *src) {
   CHECK_H(h);
   CHECK_PTR(dst, "dst");
   CHECK_PTR(src, "src");
-  return launch_CD(*h, dst, src, nullptr, h->pres_fix, implicit_coeff(*h) * h->dt, 0);
+  return launch_CD(*h, dst, src, nullptr, implicit_coeff(*h) * h->dt, 0);
 }
 int atm_vmult(atm_handle h, double *dst, const double *src) {
   CHECK_H(h);

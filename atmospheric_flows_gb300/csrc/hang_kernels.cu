@@ -19,8 +19,8 @@ int launch_B_hang(const atm_ctx &c, double *dst, const double *p, double coeff, 
 }
 
 int launch_CD_hang(const atm_ctx &c, double *dst, const double *w, const double *p,
-                   const double *pfix, double coeff, int mode) {
-  ATM_DISPATCH_K(c.k, (CD_launch<K, double, true>(schur_view(c), dst, w, p, pfix, coeff, mode)));
+                   double coeff, int mode) {
+  ATM_DISPATCH_K(c.k, (CD_launch<K, double, true>(schur_view(c), dst, w, p, coeff, mode)));
 }
 
 }  // namespace atm

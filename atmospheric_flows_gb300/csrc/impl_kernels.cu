@@ -20,7 +20,7 @@ int upload_basis_impl(const double *t) { return upload_basis_here(t); }
 // hanging-face instantiations of B and C/D live in hang_kernels.cu
 int launch_B_hang(const atm_ctx &c, double *dst, const double *p, double coeff, int mode);
 int launch_CD_hang(const atm_ctx &c, double *dst, const double *w, const double *p,
-                   const double *pfix, double coeff, int mode);
+                   double coeff, int mode);
 
 // ============================================================ mass apply ===
 // dst = M_w src for NCOMP components; weight tile (rho) or constant scale
@@ -342,8 +342,8 @@ int launch_B(const atm_ctx &c, double *dst, const double *p, double coeff, int m
   if (c.mesh.nhang > 0) return launch_B_hang(c, dst, p, coeff, mode);
   ATM_DISPATCH_K(c.k, (B_launch<K, double, false>(schur_view(c), dst, p, coeff, mode)));
 }
-int launch_CD(const atm_ctx &c, double *dst, const double *w, const double *p,
-              const double *pfix, double coeff, int mode) {
+int launch_CD(const atm_ctx &c, double *dst, const double *w, const double *p, double coeff,
+              int mode) {
   const double ns = (double)c.nc * c.nn2;
   const bool wd = (mode == 1 || mode == 2);
   // w (2 comps) + pfix read, [p], [inverse diagonal], [dst read], dst written
@@ -351,8 +351,15 @@ int launch_CD(const atm_ctx &c, double *dst, const double *w, const double *p,
   const double flops = c.nc * ((wd ? 4 : 3) * fl_eval(c.k) + fl_integrate(c.k, true) +
                                4.0 * (2 * 3 * fl_face(c.k) + fl_face(c.k)));
   TimedRegion tr(c, KF_CD, bytes, flops);
-  if (c.mesh.nhang > 0) return launch_CD_hang(c, dst, w, p, pfix, coeff, mode);
-  ATM_DISPATCH_K(c.k, (CD_launch<K, double, false>(schur_view(c), dst, w, p, pfix, coeff, mode)));
+  if (c.mesh.nhang > 0) return launch_CD_hang(c, dst, w, p, coeff, mode);
+  ATM_DISPATCH_K(c.k, (CD_launch<K, double, false>(schur_view(c), dst, w, p, coeff, mode)));
+}
+int launch_pfix_prep(const atm_ctx &c) {
+  // p_fix read; its values at the quadrature points and face traces written
+  const double bytes = 8.0 * c.nc * (c.nn2 + c.nq2 + 4.0 * c.nq);
+  const double flops = c.nc * (fl_eval(c.k) + 4.0 * fl_face(c.k));
+  TimedRegion tr(c, KF_CD, bytes, flops);
+  ATM_DISPATCH_K(c.k, (pfix_prep_launch<K, double>(schur_view(c))));
 }
 int launch_mass(const atm_ctx &c, double *dst, const double *src, int ncomp,
                 const double *weight, double scale) {
@@ -388,28 +395,33 @@ int launch_block_apply(const atm_ctx &c, double *dst, const double *src, const d
 // ---- launchers on a multigrid level (untimed; float or double) -----------
 template <typename T>
 int level_B(const LevelViewT<T> &v, T *dst, const T *p, T cB, int mode) {
-  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune};
+  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune, v.pfix, v.pfq, v.pff};
   ATM_DISPATCH_K(v.k, (B_launch<K, T, false>(o, dst, p, cB, mode)));
 }
 template <typename T>
-int level_CD(const LevelViewT<T> &v, T *dst, const T *w, const T *p, const T *pfix, T cC,
-             int mode) {
-  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune};
-  ATM_DISPATCH_K(v.k, (CD_launch<K, T, false>(o, dst, w, p, pfix, cC, mode)));
+int level_CD(const LevelViewT<T> &v, T *dst, const T *w, const T *p, T cC, int mode) {
+  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune, v.pfix, v.pfq, v.pff};
+  ATM_DISPATCH_K(v.k, (CD_launch<K, T, false>(o, dst, w, p, cC, mode)));
+}
+template <typename T>
+int level_pfix_prep(const LevelViewT<T> &v) {
+  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune, v.pfix, v.pfq, v.pff};
+  ATM_DISPATCH_K(v.k, (pfix_prep_launch<K, T>(o)));
 }
 template <typename T>
 int level_inv_diag(const LevelViewT<T> &v, T *out, T scale) {
-  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune};
+  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune, v.pfix, v.pfq, v.pff};
   ATM_DISPATCH_K(v.k, (invdiag_launch<K, T>(o, out, 1, (const T *)nullptr, scale)));
 }
 template <typename T>
 int level_block_inverse(const LevelViewT<T> &v, T *out, const T *weight) {
-  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune};
+  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune, v.pfix, v.pfq, v.pff};
   ATM_DISPATCH_K(v.k, (block_inverse_launch<K, T>(o, out, weight)));
 }
 #define ATM_LEVEL_INST(T)                                                                   \
   template int level_B<T>(const LevelViewT<T> &, T *, const T *, T, int);                   \
-  template int level_CD<T>(const LevelViewT<T> &, T *, const T *, const T *, const T *, T, int); \
+  template int level_CD<T>(const LevelViewT<T> &, T *, const T *, const T *, T, int);       \
+  template int level_pfix_prep<T>(const LevelViewT<T> &);                                   \
   template int level_inv_diag<T>(const LevelViewT<T> &, T *, T);                            \
   template int level_block_inverse<T>(const LevelViewT<T> &, T *, const T *);
 ATM_LEVEL_INST(float)

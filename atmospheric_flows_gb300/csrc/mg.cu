@@ -41,6 +41,7 @@ struct MGLevelT {
   int *ppos = nullptr;      // [nc] position a + 2b of this cell inside its parent
   int *children = nullptr;  // [nc][4] cells of level-1 (levels >= 1)
   T *ainv = nullptr, *invd = nullptr, *rho = nullptr, *pfix = nullptr;
+  T *pfq = nullptr, *pff = nullptr;  // p_fix at quadrature points / face traces
   T *x = nullptr, *b = nullptr, *r = nullptr, *t = nullptr, *d = nullptr, *wv = nullptr;
   double lam = 0.0;
 };
@@ -252,7 +253,8 @@ inline int gsz(long n) {
 
 template <typename T>
 LevelViewT<T> lview(const atm_ctx &c, const MGLevelT<T> &L) {
-  return LevelViewT<T>{c.k, L.nc, L.mesh, L.ainv, L.invd, c.stream, c.autotune && !c.capturing};
+  return LevelViewT<T>{c.k, L.nc, L.mesh, L.ainv, L.invd, c.stream, c.autotune && !c.capturing,
+                       L.pfix, L.pfq, L.pff};
 }
 
 template <typename T>
@@ -267,6 +269,7 @@ void level_free(MGLevelT<T> &L) {
   cudaFree(L.mesh.qgeo); cudaFree(L.mesh.fgeo); cudaFree(L.mesh.nbr); cudaFree(L.mesh.nbrf);
   cudaFree(L.parent); cudaFree(L.ppos); cudaFree(L.children);
   cudaFree(L.ainv); cudaFree(L.invd); cudaFree(L.rho); cudaFree(L.pfix);
+  cudaFree(L.pfq); cudaFree(L.pff);
   cudaFree(L.x); cudaFree(L.b); cudaFree(L.r); cudaFree(L.t); cudaFree(L.d); cudaFree(L.wv);
   L = MGLevelT<T>();
 }
@@ -330,6 +333,8 @@ int level_alloc(atm_ctx &c, MGLevelT<T> &L, const HostMesh &hm) {
   }
   ATM_CUDA(cudaMalloc(&L.wv, 2 * ns * sizeof(T)));
   ATM_CUDA(cudaMalloc(&L.ainv, (size_t)L.nc * nn2 * nn2 * sizeof(T)));
+  ATM_CUDA(cudaMalloc(&L.pfq, (size_t)L.nc * c.nq2 * sizeof(T)));
+  ATM_CUDA(cudaMalloc(&L.pff, (size_t)L.nc * 4 * c.nq * sizeof(T)));
   return level_inv_diag<T>(lview(c, L), L.invd, (T)(1.0 / (GAS_GAMMA - 1.0)));
 }
 
@@ -384,7 +389,7 @@ int level_apply(atm_ctx &c, MGLevelT<T> &L, T *out, const T *x) {
   TimedRegion tr(c, KF_MG_APPLY, bytes, flops);
   int rc = level_B<T>(v, L.wv, x, (T)(co * c.dt / (c.Ma * c.Ma)), 2);
   if (rc) return rc;
-  return level_CD<T>(v, out, L.wv, x, L.pfix, (T)(co * c.dt), 1);
+  return level_CD<T>(v, out, L.wv, x, (T)(co * c.dt), 1);
 }
 
 template <typename T>
@@ -506,6 +511,8 @@ int prepare(atm_ctx &c, MG &mg) {
       LAUNCHED();
     }
   }
+  for (auto &L : H.lv)
+    if ((rc = level_pfix_prep<T>(lview(c, L)))) return rc;
   if (H.rho_dirty) {
     for (auto &L : H.lv) {
       if ((rc = level_block_inverse<T>(lview(c, L), L.ainv, L.rho))) return rc;

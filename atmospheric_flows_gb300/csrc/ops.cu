@@ -75,7 +75,7 @@ int schur_apply(atm_ctx &c, double *dst, const double *p, bool precondition) {
   const double co = implicit_coeff(c);
   int rc = launch_B(c, c.wv1, p, co * c.dt / (c.Ma * c.Ma), 2);
   if (rc) return rc;
-  return launch_CD(c, dst, c.wv1, p, c.pres_fix, co * c.dt, precondition ? 2 : 1);
+  return launch_CD(c, dst, c.wv1, p, co * c.dt, precondition ? 2 : 1);
 }
 
 // Base::vmult -> apply_add (euler_operator.h:2366-2417)

@@ -121,13 +121,18 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
 template <int K, int MODE, typename T, bool HG>
 __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     k_CD(T *__restrict__ dst, const T *__restrict__ w, const T *__restrict__ p,
-         const T *__restrict__ pfix, T cC, const T *__restrict__ invd,
-         MeshT<T> mesh) {
+         const T *__restrict__ pfix, const T *__restrict__ pfq, const T *__restrict__ pff,
+         T cC, const T *__restrict__ invd, MeshT<T> mesh) {
   using C = Cfg<K>;
   constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2;
   const int CPB = blockDim.x / NQ;  // cells per block, chosen by the autotuner
   constexpr bool WITH_D = (MODE == 1 || MODE == 2);
-  constexpr int NT = WITH_D ? 4 : 3;  // w(2), pfix, [p]
+  // tiles: w(2), [p]; p_fix enters through its values at the quadrature
+  // points (pfq) and its face traces (pff), prepared when p_fix is set.  The
+  // hanging-face variant reads the p_fix tile (its traces are needed at
+  // subface points): w(2), pfix, [p].
+  constexpr int NT = (HG ? 3 : 2) + (WITH_D ? 1 : 0);
+  constexpr int TP = HG ? 3 : 2;  // tile of p
   constexpr T GM1 = GAS_GAMMA - T(1.0);
   constexpr T HG_ = GAS_GAMMA / (GAS_GAMMA - T(1.0));  // enthalpy factor
   // sign of the C contribution in dst
@@ -142,8 +147,8 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
   const int c0 = blockIdx.x * CPB;
   const int cnt = min(CPB, mesh.nc - c0);
   load_tiles<K>(tiles, NT, 0, w, 2, c0, cnt);
-  load_tiles<K>(tiles, NT, 2, pfix, 1, c0, cnt);
-  if (WITH_D) load_tiles<K>(tiles, NT, 3, p, 1, c0, cnt);
+  if (HG) load_tiles<K>(tiles, NT, 2, pfix, 1, c0, cnt);
+  if (WITH_D) load_tiles<K>(tiles, NT, TP, p, 1, c0, cnt);
   __syncthreads();
   const bool active = lc < cnt;
   const int c = c0 + lc;
@@ -154,8 +159,13 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     T wx[NQ], wz[NQ], pf[NQ], pv[NQ];
     eval_col<K>(tl, Sx, wx);
     eval_col<K>(tl + NN2, Sx, wz);
-    eval_col<K>(tl + 2 * NN2, Sx, pf);
-    if (WITH_D) eval_col<K>(tl + 3 * NN2, Sx, pv);
+    if (HG) {
+      eval_col<K>(tl + 2 * NN2, Sx, pf);
+    } else {
+#pragma unroll
+      for (int qz = 0; qz < NQ; ++qz) pf[qz] = pfq[(long)c * NQ2 + qz * NQ + col];
+    }
+    if (WITH_D) eval_col<K>(tl + TP * NN2, Sx, pv);
     const T *G = mesh.qgeo + (long)c * 5 * NQ2;
     T V[NQ], Gxi[NQ], Get[NQ];
 #pragma unroll
@@ -178,10 +188,16 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
         return;
       }
       const T wxp = face_val<K>(tl, f, Ro), wzp = face_val<K>(tl + NN2, f, Ro);
-      const T pfp = face_val<K>(tl + 2 * NN2, f, Ro);
       const T wxm = face_val<K>(w + (long)nb * 2 * NN2, nf, Rn);
       const T wzm = face_val<K>(w + ((long)nb * 2 + 1) * NN2, nf, Rn);
-      const T pfm = face_val<K>(pfix + (long)nb * NN2, nf, Rn);
+      T pfp, pfm;
+      if (HG) {
+        pfp = face_val<K>(tl + 2 * NN2, f, Ro);
+        pfm = face_val<K>(pfix + (long)nb * NN2, nf, Rn);
+      } else {  // conforming: face point col of both sides coincide
+        pfp = pff[((long)c * 4 + f) * NQ + col];
+        pfm = pff[((long)nb * 4 + nf) * NQ + col];
+      }
       const T av0 = T(0.5) * HG_ * (pfp * wxp + pfm * wxm);
       const T av1 = T(0.5) * HG_ * (pfp * wzp + pfm * wzm);
       const T lam = fmax(fabs(wxp * n0 + wzp * n1), fabs(wxm * n0 + wzm * n1));
@@ -207,6 +223,35 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
   }
 }
 
+// ========================================================== p_fix prep ===
+// Values of p_fix at the quadrature points, pfq[c][qz][qx], and its traces
+// on the four faces, pff[c][f][q]: the C/D kernel's p_fix input, computed
+// once per p_fix instead of once per Schur apply.
+template <int K, typename T>
+__global__ void __launch_bounds__(Cfg<K>::THREADS)
+    k_pfix_prep(T *__restrict__ pfq, T *__restrict__ pff, const T *__restrict__ pfix,
+                MeshT<T> mesh) {
+  using C = Cfg<K>;
+  constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2, CPB = C::CPB;
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  T *tiles = reinterpret_cast<T *>(sm_raw);
+  const int tid = threadIdx.x, lc = tid / NQ, col = tid - lc * NQ;
+  const int c0 = blockIdx.x * CPB;
+  const int cnt = min(CPB, mesh.nc - c0);
+  load_tiles<K>(tiles, 1, 0, pfix, 1, c0, cnt);
+  __syncthreads();
+  if (lc >= cnt) return;
+  const int c = c0 + lc;
+  const T *tl = tiles + lc * NN2;
+  T Sx[NN], Dx[NN], v[NQ];
+  load_rows<K>(col, Sx, Dx);
+  eval_col<K>(tl, Sx, v);
+#pragma unroll
+  for (int qz = 0; qz < NQ; ++qz) pfq[(long)c * NQ2 + qz * NQ + col] = v[qz];
+#pragma unroll
+  for (int f = 0; f < 4; ++f) pff[((long)c * 4 + f) * NQ + col] = face_val<K>(tl, f, Sx);
+}
+
 // ============================================================ launchers ===
 template <typename T>
 struct OpView {
@@ -216,11 +261,12 @@ struct OpView {
   const T *invd;
   cudaStream_t st;
   bool tune;  // the autotuner may time tile shapes on this stream
+  const T *pfix, *pfq, *pff;  // frozen p_fix and its prepared values (C/D)
 };
 
 inline OpView<double> schur_view(const atm_ctx &c) {
   return OpView<double>{c.k, c.nc, c.mesh, c.ainv, c.invdiag_D, c.stream,
-                        c.autotune && !c.capturing};
+                        c.autotune && !c.capturing, c.pres_fix, c.pfq, c.pff};
 }
 
 template <int K, typename T, bool HG>
@@ -246,21 +292,32 @@ int B_launch(const OpView<T> &v, T *dst, const T *p, T cB, int mode) {
   return ATM_OK;
 }
 
+template <int K, typename T>
+int pfix_prep_launch(const OpView<T> &v) {
+  using C = Cfg<K>;
+  const int grid = (v.nc + C::CPB - 1) / C::CPB;
+  k_pfix_prep<K, T><<<grid, C::THREADS, sizeof(T) * C::CPB * C::NN2, v.st>>>(
+      const_cast<T *>(v.pfq), const_cast<T *>(v.pff), v.pfix, v.mesh);
+  ATM_CHECK_LAUNCH("k_pfix_prep");
+  return ATM_OK;
+}
+
 template <int K, typename T, bool HG>
-int CD_launch(const OpView<T> &v, T *dst, const T *w, const T *p, const T *pfix, T cC,
-              int mode) {
+int CD_launch(const OpView<T> &v, T *dst, const T *w, const T *p, T cC, int mode) {
+  const T *pfix = v.pfix;
   using C = Cfg<K>;
   auto launch = [&](int cpb) -> cudaError_t {
     const int grid = (v.nc + cpb - 1) / cpb, th = cpb * C::NQ;
     const size_t sm = smem_bytes<K, T>(cpb, 4, 1, HG);
-    void (*fn)(T *, const T *, const T *, const T *, T, const T *, MeshT<T>) =
+    void (*fn)(T *, const T *, const T *, const T *, const T *, const T *, T, const T *,
+               MeshT<T>) =
         mode == 0 ? k_CD<K, 0, T, HG>
                   : (mode == 1 ? k_CD<K, 1, T, HG> : (mode == 2 ? k_CD<K, 2, T, HG> : k_CD<K, 3, T, HG>));
     if (sm > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
       if (e != cudaSuccess) return e;
     }
-    fn<<<grid, th, sm, v.st>>>(dst, w, p, pfix, cC, v.invd, v.mesh);
+    fn<<<grid, th, sm, v.st>>>(dst, w, p, pfix, v.pfq, v.pff, cC, v.invd, v.mesh);
     return cudaGetLastError();
   };
   // mode 3 (dst -= C w) is not idempotent: it uses the choice made for mode 0

@@ -85,7 +85,7 @@ extern "C" int atm_schur_vmult_static_scratch(atm_handle h, double *dst, const d
   const bool tune = h->autotune;
   h->autotune = false;
   rc = launch_B(*h, scratch, src, co * h->dt / (h->Ma * h->Ma), 2);
-  if (rc == ATM_OK) rc = launch_CD(*h, dst, scratch, src, h->pres_fix, co * h->dt, 1);
+  if (rc == ATM_OK) rc = launch_CD(*h, dst, scratch, src, co * h->dt, 1);
   h->autotune = tune;
   return rc;
 }

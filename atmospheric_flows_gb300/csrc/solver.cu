@@ -75,6 +75,7 @@ int update_density(atm_ctx &c, Solver &s) {
 int pressure_fixed_point(atm_ctx &c, Solver &s) {
   const long ns = c.n_scalar();
   TRY(vec_copy(c.stream, c.pres_fix, s.pres_fixed_old, ns));  // set_pres_fixed
+  TRY(launch_pfix_prep(c));
   const StageCoef co = stage_coef_flux(c, c.hstage);
   if (c.hstage == 1) {
     const double *sp[] = {s.rho_old, s.u_old, s.pres_old, s.rho_tmp_2, s.u_fixed};
@@ -92,7 +93,7 @@ int pressure_fixed_point(atm_ctx &c, Solver &s) {
   // tmp_1 = A^{-1} rhs_u ; rhs_pres -= C tmp_1
   TRY(launch_block_apply(c, s.tmp_1, s.rhs_u, c.ainv, 2, 1.0));
   const double cc = implicit_coeff(c);
-  TRY(launch_CD(c, s.rhs_pres, s.tmp_1, nullptr, c.pres_fix, cc * c.dt, 3));
+  TRY(launch_CD(c, s.rhs_pres, s.tmp_1, nullptr, cc * c.dt, 3));
   TRY(vec_dot(c.stream, s.rhs_pres, s.rhs_pres, ns, c.red, c.red_out));
   TRY(read_scalars(c, 1));
   const double tol = s.eps * std::sqrt(c.h_red[0]);
