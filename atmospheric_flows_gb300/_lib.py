@@ -73,7 +73,8 @@ SIGNATURES = {
 }
 
 KERNEL_FAMILIES = ("rhs_rho", "rhs_vel", "rhs_pres", "B", "CD", "mass", "diag",
-                   "block_inverse", "block_apply", "mg_level_apply", "mg_vcycle")
+                   "block_inverse", "block_apply", "mg_level_apply", "mg_vcycle",
+                   "pfix_prep")
 
 STATUS = {0: "OK", 1: "BAD_ARG", 2: "NOT_CONVERGED", 3: "NONFINITE", 4: "OOM", 5: "TIMEOUT",
           6: "CUDA_ERROR", 7: "NOT_READY"}

@@ -39,7 +39,7 @@ struct StageCoef {
 // Kernel families timed by the optional per-launch CUDA-event timers.
 enum KFam {
   KF_RHS_RHO = 0, KF_RHS_VEL, KF_RHS_PRES, KF_B, KF_CD, KF_MASS, KF_DIAG, KF_BLOCK_INV,
-  KF_BLOCK_APPLY, KF_MG_APPLY, KF_MG_OTHER, KF_COUNT
+  KF_BLOCK_APPLY, KF_MG_APPLY, KF_MG_OTHER, KF_PFIX_PREP, KF_COUNT
 };
 
 // CUDA-event timers around operator launches (off unless enabled).

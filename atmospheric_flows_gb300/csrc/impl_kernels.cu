@@ -358,7 +358,7 @@ int launch_pfix_prep(const atm_ctx &c) {
   // p_fix read; its values at the quadrature points and face traces written
   const double bytes = 8.0 * c.nc * (c.nn2 + c.nq2 + 4.0 * c.nq);
   const double flops = c.nc * (fl_eval(c.k) + 4.0 * fl_face(c.k));
-  TimedRegion tr(c, KF_CD, bytes, flops);
+  TimedRegion tr(c, KF_PFIX_PREP, bytes, flops);
   ATM_DISPATCH_K(c.k, (pfix_prep_launch<K, double>(schur_view(c))));
 }
 int launch_mass(const atm_ctx &c, double *dst, const double *src, int ncomp,

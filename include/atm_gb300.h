@@ -89,9 +89,10 @@ long atm_n_scalar(atm_handle h);
  * 249).  atm_kernel_launches counts every kernel launch of the library in
  * this process.  With timing enabled, each operator launch is bracketed by
  * CUDA events on the context's stream; atm_timing_read synchronises and
- * returns, per family 0..10 = rhs_rho, rhs_vel, rhs_pres, B, C/D, mass,
+ * returns, per family 0..11 = rhs_rho, rhs_vel, rhs_pres, B, C/D, mass,
  * diagonal, block inverse, block apply, multigrid level Schur apply (B+C/D
- * pair, any level), whole V-cycle (nested: contains the level applies):
+ * pair, any level), whole V-cycle (nested: contains the level applies),
+ * p_fix preparation for C/D (values at quadrature points, face traces):
  * total ms, launches, algorithmic HBM
  * bytes (fields read + written, 8 B per node value) and FP64 flops of the
  * sum-factorisation contractions; then resets them.  Any output may be NULL. */
