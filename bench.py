@@ -165,7 +165,7 @@ FP64_PEAK_TFLOPS = 1.255
 # from `ncu` captures of this bench at 320x160 (profiles/k_CD_q4_320x160.md,
 # profiles/k_B_q4_320x160.md);
 # the traffic grows in proportion to the cell count.
-NCU_TRAFFIC_PER_CELL = {4: {"CD": 273.1e6 / 51200, "B": 469.6e6 / 51200}}
+NCU_TRAFFIC_PER_CELL = {4: {"CD": 311.0e6 / 51200, "B": 469.6e6 / 51200}}
 
 
 def cpu_baseline(case, eps):
