@@ -29,8 +29,8 @@ import math
 
 import numpy as np
 
-from .hill import (CP, G_GRAV, GAMMA, MACH, P0, R_GAS, RHO_REF, HillCase, HillParams,
-                   background, build_case, build_mesh, gll_points, lagrange_matrix)
+from .hill import (CP, GAMMA, MACH, P0, R_GAS, RHO_REF, HillCase, HillParams, background,
+                   build_case, build_mesh, gll_points, lagrange_matrix)
 
 _OPP = (1, 0, 3, 2)
 

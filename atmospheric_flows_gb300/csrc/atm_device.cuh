@@ -448,15 +448,6 @@ __device__ __forceinline__ void face_terms(const MeshT<T> &mesh, int c, int col,
   }
 }
 
-// add the face values of the output column t (conforming or with hanging faces)
-template <int K, bool HG, typename T>
-__device__ __forceinline__ void add_faces(const MeshT<T> &mesh, int c, const T *__restrict__ F,
-                                          const T *__restrict__ Fh, int t,
-                                          const T (&St)[2 * K + 1], T (&out)[K + 1]) {
-  if (HG) add_face_out_hg<K>(F, Fh, hanging_mask(mesh, c), t, St, out);
-  else add_face_out<K>(F, t, St, out);
-}
-
 template <int K, bool HG, typename T>
 __device__ __forceinline__ void output_phase(const MeshT<T> &mesh, int c, const T *__restrict__ xa,
                                              const T *__restrict__ xb, const T *__restrict__ F,

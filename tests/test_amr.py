@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from atmospheric_flows_gb300 import amr
-from atmospheric_flows_gb300.hill import HillParams, build_case, build_mesh, map_points
+from atmospheric_flows_gb300.hill import HillParams, build_case, build_mesh
 from oracle.oracle import OracleOperator
 
 
