@@ -83,6 +83,47 @@ def dist_env():
     return ws, rank, local
 
 
+class RankGroup:
+    """Barrier and max-over-ranks of the timing, on an initialised process
+    group (NCCL on the GPUs; any backend works).  With one rank both are
+    local.  `device` is where the reduction tensor lives ("cuda" or "cpu");
+    on "cuda" the barrier also synchronises the device on both sides."""
+
+    def __init__(self, world_size, device="cuda"):
+        self.ws = int(world_size)
+        self.device = device
+
+    def _sync(self):
+        if self.device == "cuda":
+            import torch
+
+            torch.cuda.synchronize()
+
+    def barrier(self):
+        self._sync()
+        if self.ws > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+            self._sync()
+
+    def max(self, x):
+        if self.ws == 1:
+            return x
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([float(x)], dtype=torch.float64, device=self.device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+
+def aggregate_rate(world_size, units_per_rank_per_step, steps, max_ms):
+    """Whole-job throughput: the units every rank processed over the slowest
+    rank's time (weak scaling: each rank advances its own member)."""
+    return world_size * units_per_rank_per_step * steps / (max_ms * 1e-3)
+
+
 def workload(args):
     return {"workload": f"flow-over-hill {args.nx}x{args.nz} Q{args.degree} FP64, acoustic "
                         f"CFL {args.cfl:g}, reference solver (GMRES + Jacobi, eps 1e-8)",
@@ -268,21 +309,11 @@ def run_gb300(args):
 
     case = build_case(HillParams(nx=args.nx, nz=args.nz, degree=args.degree, cfl=args.cfl))
 
-    def barrier():
-        torch.cuda.synchronize()
-        if ws > 1:
-            torch.distributed.barrier()
-            torch.cuda.synchronize()
-
-    def max_over_ranks(x):
-        if ws > 1:
-            t = torch.tensor([x], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            return float(t.item())
-        return x
+    group = RankGroup(ws, "cuda")
+    barrier = group.barrier
 
     def rate(ms):
-        return ws * case.n_dofs * args.steps / (max_over_ranks(ms) * 1e-3)
+        return aggregate_rate(ws, case.n_dofs, args.steps, group.max(ms))
 
     # ---- headline: the reference's solver and tolerance on the GPU --------
     with ClockSampler(local) as clk:
@@ -307,7 +338,7 @@ def run_gb300(args):
         _lib.call("atm_solver_run", h, 1)
         _lib.call("atm_solver_get_state", h, *ptrs)
     barrier()
-    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_s = group.max(time.perf_counter() - t0)
     e2e = {"value": ws * case.n_dofs * args.steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": int(8 * 4 * ns), "d2h_bytes_per_step": int(8 * 4 * ns)}
     solver.close()
