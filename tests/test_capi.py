@@ -12,7 +12,8 @@ HEADER = os.path.join(ROOT, "include", "atm_gb300.h")
 
 
 def declared():
-    src = open(HEADER).read()
+    with open(HEADER) as fh:
+        src = fh.read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     return sorted(set(re.findall(r"\b(atm_[a-z0-9_]+)\s*\(", src)))
 
