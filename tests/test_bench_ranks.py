@@ -41,7 +41,7 @@ def _rank_main(rank, world, port, out):
 def test_two_gloo_ranks_take_the_slowest_time():
     world = 2
     port = _free_port()
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:
         out = mgr.dict()
         mp.spawn(_rank_main, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)

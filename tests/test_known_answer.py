@@ -1,0 +1,98 @@
+"""Known-answer tests of the whole IMEX time loop against analytic solutions.
+
+The reference ships no golden data and cannot be built here (deal.II), so
+besides the discrete identities of test_oracle.py the oracle -- and the GPU
+path through it -- is pinned by two analytic solutions of the compressible
+Euler equations in the reference's scaling (Ma = 1/sqrt(R T_ref), gravity
+off):
+
+* a uniform free stream on a flat periodic channel with walls is an exact
+  steady solution; the scheme keeps it to round-off;
+* a small-amplitude acoustic wave p = 1 + e cos(2 pi (x - c t)/L),
+  c^2 = gamma p0 / (rho0 Ma^2), with the matching density and velocity
+  (linear acoustics), returns to its initial state after one period; with
+  dt proportional to h the error falls at the IMEX scheme's second order
+  until the amplitude's nonlinearity and the Picard tolerance (1e-10 of the
+  total pressure, Atmospheric_Flow.cc:1135-1153) set a floor near 1e-3 e.
+"""
+import dataclasses
+import math
+
+import numpy as np
+import pytest
+
+from atmospheric_flows_gb300.hill import GAMMA, MACH, HillParams, build_case
+from oracle.oracle import OracleSolver
+
+L_X, H_Z, AMP = 1000.0, 250.0, 1e-4
+
+
+def free_stream_case():
+    c0 = build_case(HillParams(nx=6, nz=3, degree=3, h0=0.0, cfl=2.0))
+    u = np.zeros((c0.n_cells, 2, 16))
+    u[:, 0, :] = 10.0
+    return dataclasses.replace(c0, rho=np.full_like(c0.rho, 1.2), u=u.reshape(-1),
+                               p=np.full_like(c0.p, 0.9), Fr=1e30,
+                               sponge_alpha=np.zeros_like(c0.rho))
+
+
+def acoustic_case(nx, k):
+    """Right-moving linear acoustic wave on a flat x-periodic channel."""
+    c0 = build_case(HillParams(nx=nx, nz=1, degree=k, x0=0.0, x1=L_X, height=H_Z, h0=0.0,
+                               cfl=1.0))
+    x = c0.node_xz[..., 0].reshape(-1)
+    c = math.sqrt(GAMMA / MACH ** 2)  # rho0 = p0 = 1
+    f = np.cos(2.0 * math.pi * x / L_X)
+    u = np.zeros((c0.n_cells, 2, (k + 1) ** 2))
+    u[:, 0, :] = (AMP / (MACH ** 2 * c) * f).reshape(c0.n_cells, -1)
+    case = dataclasses.replace(c0, rho=1.0 + AMP / (MACH ** 2 * c ** 2) * f, u=u.reshape(-1),
+                               p=1.0 + AMP * f, Fr=1e30, sponge_alpha=np.zeros_like(x))
+    period = L_X / c
+    return case, period
+
+
+def acoustic_error(solver_cls, nx, k, steps_per_cell=5, **kw):
+    case, period = acoustic_case(nx, k)
+    n = steps_per_cell * nx
+    s = solver_cls(case, eps=1e-12, dt=period / n, **kw)
+    s.run(n)
+    _, _, p = s.get_state()
+    return float(np.max(np.abs(p - case.p)) / AMP), s
+
+
+def test_free_stream_is_preserved_exactly():
+    case = free_stream_case()
+    s = OracleSolver(case, eps=1e-12, inner_tol=1e-14)
+    s.run(3)
+    rho, u, p = s.get_state()
+    assert np.max(np.abs(rho - 1.2)) < 1e-13
+    assert np.max(np.abs(u - case.u)) < 1e-12
+    assert np.max(np.abs(p - 0.9)) < 1e-13
+
+
+@pytest.mark.parametrize("k,meshes", [(1, (8, 16, 32)), (2, (4, 8, 16))])
+def test_acoustic_wave_converges_at_second_order(k, meshes):
+    errs = [acoustic_error(OracleSolver, nx, k, inner_tol=1e-14)[0] for nx in meshes]
+    orders = [math.log2(a / b) for a, b in zip(errs, errs[1:])]
+    assert errs[-1] < 0.03, errs
+    assert min(orders) > 1.8, (errs, orders)
+
+
+@pytest.mark.gpu
+def test_gpu_free_stream_and_acoustic_wave(cuda_ok):
+    from atmospheric_flows_gb300.euler_solver import EulerSolver
+
+    case = free_stream_case()
+    g = EulerSolver(case, eps=1e-12)
+    g.run(3)
+    rho, u, p = g.get_state()
+    assert np.max(np.abs(rho - 1.2)) < 1e-13
+    assert np.max(np.abs(p - 0.9)) < 1e-13
+    g.close()
+    e_gpu, g = acoustic_error(EulerSolver, 16, 2)
+    e_orc, o = acoustic_error(OracleSolver, 16, 2, inner_tol=1e-15)
+    assert e_gpu < 0.005
+    # the two paths agree far below the discretisation error
+    for a, b in zip(g.get_state(), o.get_state()):
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-10
+    g.close()
