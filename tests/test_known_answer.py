@@ -96,7 +96,10 @@ def test_gpu_free_stream_and_acoustic_wave(cuda_ok):
     e_gpu, g = acoustic_error(EulerSolver, 16, 2)
     e_orc, o = acoustic_error(OracleSolver, 16, 2, inner_tol=1e-15)
     assert e_gpu < 0.005
-    # the two paths agree far below the discretisation error
+    assert abs(e_gpu - e_orc) < 0.1 * e_orc
+    # The Picard loop stops on 1e-10 of the total pressure per step, so over
+    # these 80 steps the two paths separate by ~1e-10 per step (5e-9 in rho
+    # measured); still far below the discretisation error.
     for a, b in zip(g.get_state(), o.get_state()):
-        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-10
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-7
     g.close()
