@@ -232,6 +232,18 @@ template <typename T>
 int level_B(const LevelViewT<T> &v, T *dst, const T *p, T cB, int mode);
 template <typename T>
 int level_CD(const LevelViewT<T> &v, T *dst, const T *w, const T *p, T cC, int mode);
+// Chebyshev update fused into the C/D epilogue (multigrid smoother): with
+// t = S x computed by the kernel, r = rhs - t, d = (first ? 0 : a d) + b invd r,
+// x += d.  x is also the kernel's D input, read for the cell's own nodes only.
+template <typename T>
+struct ChebArgs {
+  T *x = nullptr, *d = nullptr;
+  const T *rhs = nullptr;
+  T a = T(0), b = T(0);
+  int first = 0;
+};
+template <typename T>
+int level_CD_cheb(const LevelViewT<T> &v, const T *w, T cC, const ChebArgs<T> &ch);
 template <typename T>
 int level_pfix_prep(const LevelViewT<T> &v);
 template <typename T>

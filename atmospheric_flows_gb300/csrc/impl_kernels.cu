@@ -17,7 +17,7 @@ namespace atm {
 
 int upload_basis_impl(const double *t) { return upload_basis_here(t); }
 
-// hanging-face instantiations of B and C/D live in hang_kernels.cu
+// hanging-face instantiations of B and C/D live in hang_schur.cu
 int launch_B_hang(const atm_ctx &c, double *dst, const double *p, double coeff, int mode);
 int launch_CD_hang(const atm_ctx &c, double *dst, const double *w, const double *p,
                    double coeff, int mode);
@@ -404,6 +404,11 @@ int level_CD(const LevelViewT<T> &v, T *dst, const T *w, const T *p, T cC, int m
   ATM_DISPATCH_K(v.k, (CD_launch<K, T, false>(o, dst, w, p, cC, mode)));
 }
 template <typename T>
+int level_CD_cheb(const LevelViewT<T> &v, const T *w, T cC, const ChebArgs<T> &ch) {
+  OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune, v.pfix, v.pfq, v.pff};
+  ATM_DISPATCH_K(v.k, (CD_launch<K, T, false>(o, nullptr, w, ch.x, cC, 4, &ch)));
+}
+template <typename T>
 int level_pfix_prep(const LevelViewT<T> &v) {
   OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune, v.pfix, v.pfq, v.pff};
   ATM_DISPATCH_K(v.k, (pfix_prep_launch<K, T>(o)));
@@ -422,6 +427,7 @@ int level_block_inverse(const LevelViewT<T> &v, T *out, const T *weight) {
   template int level_B<T>(const LevelViewT<T> &, T *, const T *, T, int);                   \
   template int level_CD<T>(const LevelViewT<T> &, T *, const T *, const T *, T, int);       \
   template int level_pfix_prep<T>(const LevelViewT<T> &);                                   \
+  template int level_CD_cheb<T>(const LevelViewT<T> &, const T *, T, const ChebArgs<T> &);   \
   template int level_inv_diag<T>(const LevelViewT<T> &, T *, T);                            \
   template int level_block_inverse<T>(const LevelViewT<T> &, T *, const T *);
 ATM_LEVEL_INST(float)

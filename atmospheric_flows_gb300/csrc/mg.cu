@@ -392,6 +392,32 @@ int level_apply(atm_ctx &c, MGLevelT<T> &L, T *out, const T *x) {
   return level_CD<T>(v, out, L.wv, x, (T)(co * c.dt), 1);
 }
 
+// One Chebyshev step on level L fused with its operator: t = S_l x (B, then
+// C/D), r = b - t, d = (first ? 0 : a d) + b_coef invd r, x += d; the C/D
+// kernel does the update in its epilogue instead of storing t.
+template <typename T>
+int level_apply_cheb(atm_ctx &c, MGLevelT<T> &L, double a, double b_coef, bool first) {
+  const double co = implicit_coeff(c);
+  LevelViewT<T> v = lview(c, L);
+  const double ns = (double)L.nc * c.nn2, sz = sizeof(T);
+  // as level_apply, plus rhs, invd, d read and d, x written in the update
+  const double bytes = sz * (ns * (1 + 2 + 2 + 1 + 1 + 5) + (double)L.nc * c.nn2 * c.nn2);
+  const double flops = L.nc * (fl_eval(c.k) + 2 * fl_integrate(c.k, true) + 4.0 * 4 * fl_face(c.k) +
+                               4.0 * c.nn2 * c.nn2 + 4 * fl_eval(c.k) + fl_integrate(c.k, true) +
+                               4.0 * 7 * fl_face(c.k));
+  TimedRegion tr(c, KF_MG_APPLY, bytes, flops);
+  int rc = level_B<T>(v, L.wv, L.x, (T)(co * c.dt / (c.Ma * c.Ma)), 2);
+  if (rc) return rc;
+  ChebArgs<T> ch;
+  ch.x = L.x;
+  ch.d = L.d;
+  ch.rhs = L.b;
+  ch.a = (T)a;
+  ch.b = (T)b_coef;
+  ch.first = first ? 1 : 0;
+  return level_CD_cheb<T>(v, L.wv, (T)(co * c.dt), ch);
+}
+
 template <typename T>
 int nrm2(atm_ctx &c, const T *v, long n, double *out_host) {
   k_nrm2_partial<T><<<NB, 256, 0, c.stream>>>(v, n, c.red);
@@ -444,18 +470,12 @@ int chebyshev(atm_ctx &c, MGLevelT<T> &L, int degree, double range, bool zero_st
     k_cheb<T><<<gsz(n), 256, 0, c.stream>>>(L.x, L.d, L.b, L.t, L.invd, T(0),
                                              (T)(1.0 / theta), 1, 0, n);
     LAUNCHED();
-  } else {
-    if ((rc = level_apply<T>(c, L, L.t, L.x))) return rc;
-    k_cheb<T><<<gsz(n), 256, 0, c.stream>>>(L.x, L.d, L.b, L.t, L.invd, T(0),
-                                             (T)(1.0 / theta), 0, 1, n);
-    LAUNCHED();
+  } else if ((rc = level_apply_cheb<T>(c, L, 0.0, 1.0 / theta, true))) {
+    return rc;
   }
   for (int k = 1; k < degree; ++k) {
-    if ((rc = level_apply<T>(c, L, L.t, L.x))) return rc;
     const double rho_new = 1.0 / (2.0 * sigma - rho);
-    k_cheb<T><<<gsz(n), 256, 0, c.stream>>>(L.x, L.d, L.b, L.t, L.invd, (T)(rho_new * rho),
-                                             (T)(2.0 * rho_new / delta), 0, 2, n);
-    LAUNCHED();
+    if ((rc = level_apply_cheb<T>(c, L, rho_new * rho, 2.0 * rho_new / delta, false))) return rc;
     rho = rho_new;
   }
   return ATM_OK;

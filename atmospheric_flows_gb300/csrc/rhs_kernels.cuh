@@ -1,7 +1,7 @@
 // Explicit IMEX stage right-hand sides (FP64), one kernel per equation,
 // templated on the polynomial degree K, the IMEX stage ST and HG (mesh with
 // hanging faces).  Included by rhs_kernels.cu (HG = false) and
-// hang_kernels.cu (HG = true), so the two families compile in parallel.
+// hang_rhs_*.cu / hang_schur.cu (HG = true), so the two families compile in parallel.
 //
 //   rho      : euler_operator.h:344-473 (cell), 478-692 (face), no boundary
 //   momentum : euler_operator.h:1622-1886 (cell), 1891-2184 (face),
@@ -402,20 +402,23 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
 }
 
 // ============================================================ launchers ===
-template <int K, bool HG>
-int rhs_launch(const atm_ctx &c, int kind, int stage, double *dst, const double *const *src,
+// KIND 0 density, 1 momentum, 2 energy (a template parameter, so each kind's
+// kernels can be instantiated in a translation unit of its own)
+template <int K, bool HG, int KIND>
+int rhs_launch(const atm_ctx &c, int stage, double *dst, const double *const *src,
                const StageCoef &co) {
   using C = Cfg<K>;
+  constexpr int kind = KIND;
   SrcPtrs sp{};
   const int nsrc_tab[3][3] = {{2, 4, 6}, {4, 7, 9}, {5, 8, 11}};
   const int nsrc = nsrc_tab[kind][stage - 1];
   for (int i = 0; i < nsrc; ++i) sp.p[i] = src[i];
   int ntile;
   void (*fn)(double *, SrcPtrs, StageCoef, Mesh) = nullptr;
-  if (kind == 0) {
+  if constexpr (KIND == 0) {
     ntile = 3 * stage;
     fn = stage == 1 ? k_rhs_rho<K, 1, HG> : (stage == 2 ? k_rhs_rho<K, 2, HG> : k_rhs_rho<K, 3, HG>);
-  } else if (kind == 1) {
+  } else if constexpr (KIND == 1) {
     ntile = 4 * stage + (stage < 3 ? 1 : 0);
     fn = stage == 1 ? k_rhs_vel<K, 1, HG> : (stage == 2 ? k_rhs_vel<K, 2, HG> : k_rhs_vel<K, 3, HG>);
   } else {
@@ -452,16 +455,16 @@ int rhs_launch(const atm_ctx &c, int kind, int stage, double *dst, const double 
   return ATM_OK;
 }
 
-template <bool HG>
-int rhs_dispatch_t(const atm_ctx &c, int kind, int stage, double *dst, const double *const *src,
-                   const StageCoef &co) {
+template <bool HG, int KIND>
+int rhs_dispatch_kind(const atm_ctx &c, int stage, double *dst, const double *const *src,
+                      const StageCoef &co) {
   if (stage < 1 || stage > 3) return ATM_BAD_ARG;
   switch (c.k) {
-    case 1: return rhs_launch<1, HG>(c, kind, stage, dst, src, co);
-    case 2: return rhs_launch<2, HG>(c, kind, stage, dst, src, co);
-    case 3: return rhs_launch<3, HG>(c, kind, stage, dst, src, co);
-    case 4: return rhs_launch<4, HG>(c, kind, stage, dst, src, co);
-    case 5: return rhs_launch<5, HG>(c, kind, stage, dst, src, co);
+    case 1: return rhs_launch<1, HG, KIND>(c, stage, dst, src, co);
+    case 2: return rhs_launch<2, HG, KIND>(c, stage, dst, src, co);
+    case 3: return rhs_launch<3, HG, KIND>(c, stage, dst, src, co);
+    case 4: return rhs_launch<4, HG, KIND>(c, stage, dst, src, co);
+    case 5: return rhs_launch<5, HG, KIND>(c, stage, dst, src, co);
     default: return ATM_BAD_ARG;
   }
 }

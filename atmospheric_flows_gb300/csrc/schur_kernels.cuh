@@ -5,7 +5,7 @@
 //   C   euler_operator.h:1413-1507
 //   D   euler_operator.h:1386-1408
 // HG selects the face loop with hanging faces (2:1 adaptive meshes).
-// Included by impl_kernels.cu (HG = false) and hang_kernels.cu (HG = true).
+// Included by impl_kernels.cu (HG = false) and hang_rhs_*.cu / hang_schur.cu (HG = true).
 #pragma once
 #include "atm_device.cuh"
 
@@ -118,15 +118,17 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
 // ===================================================================== CD ===
 // MODE 0: dst = C w ; 1: dst = sD D p - C w ; 2: dst = invd .* (sD D p - C w)
 // MODE 3: dst -= C w
+// MODE 4: t = sD D p - C w with p = ch.x, then the Chebyshev update of ch
+//         (x and d, with rhs and invd) instead of a store of t
 template <int K, int MODE, typename T, bool HG>
 __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     k_CD(T *__restrict__ dst, const T *__restrict__ w, const T *__restrict__ p,
          const T *__restrict__ pfix, const T *__restrict__ pfq, const T *__restrict__ pff,
-         T cC, const T *__restrict__ invd, MeshT<T> mesh) {
+         T cC, const T *__restrict__ invd, MeshT<T> mesh, ChebArgs<T> ch) {
   using C = Cfg<K>;
   constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2;
   const int CPB = blockDim.x / NQ;  // cells per block, chosen by the autotuner
-  constexpr bool WITH_D = (MODE == 1 || MODE == 2);
+  constexpr bool WITH_D = (MODE == 1 || MODE == 2 || MODE == 4);
   // tiles: w(2), [p]; p_fix enters through its values at the quadrature
   // points (pfq) and its face traces (pff), prepared when p_fix is set.  The
   // hanging-face variant reads the p_fix tile (its traces are needed at
@@ -212,13 +214,23 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     const T *xa = xab + lc * 2 * NN * NQ;
     output_phase<K, HG>(mesh, c, xa, xa + NN * NQ, fb + lc * 4 * NQ, fh + lc * 4 * NQ, col, St, Dt,
                         out);
-    T *d = dst + (long)c * NN2;
+    T *d = MODE == 4 ? nullptr : dst + (long)c * NN2;
 #pragma unroll
     for (int iz = 0; iz < NN; ++iz) {
       const int i = out_node<K, HG>(col, iz);
-      if (MODE == 2) d[i] = invd[(long)c * NN2 + i] * out[iz];
-      else if (MODE == 3) d[i] -= out[iz];
-      else d[i] = out[iz];
+      if (MODE == 2) {
+        d[i] = invd[(long)c * NN2 + i] * out[iz];
+      } else if (MODE == 3) {
+        d[i] -= out[iz];
+      } else if (MODE == 4) {
+        const long g = (long)c * NN2 + i;
+        const T r = ch.rhs[g] - out[iz];
+        const T dk = (ch.first ? T(0) : ch.a * ch.d[g]) + ch.b * invd[g] * r;
+        ch.d[g] = dk;
+        ch.x[g] = ch.x[g] + dk;
+      } else {
+        d[i] = out[iz];
+      }
     }
   }
 }
@@ -303,27 +315,35 @@ int pfix_prep_launch(const OpView<T> &v) {
 }
 
 template <int K, typename T, bool HG>
-int CD_launch(const OpView<T> &v, T *dst, const T *w, const T *p, T cC, int mode) {
+int CD_launch(const OpView<T> &v, T *dst, const T *w, const T *p, T cC, int mode,
+              const ChebArgs<T> *cheb = nullptr) {
   const T *pfix = v.pfix;
+  const ChebArgs<T> ch = cheb ? *cheb : ChebArgs<T>{};
   using C = Cfg<K>;
   auto launch = [&](int cpb) -> cudaError_t {
     const int grid = (v.nc + cpb - 1) / cpb, th = cpb * C::NQ;
     const size_t sm = smem_bytes<K, T>(cpb, 4, 1, HG);
     void (*fn)(T *, const T *, const T *, const T *, const T *, const T *, T, const T *,
-               MeshT<T>) =
+               MeshT<T>, ChebArgs<T>) =
         mode == 0 ? k_CD<K, 0, T, HG>
-                  : (mode == 1 ? k_CD<K, 1, T, HG> : (mode == 2 ? k_CD<K, 2, T, HG> : k_CD<K, 3, T, HG>));
+        : mode == 1 ? k_CD<K, 1, T, HG>
+        : mode == 2 ? k_CD<K, 2, T, HG>
+                    : k_CD<K, 3, T, HG>;
+    if constexpr (!HG) {  // the fused smoother step runs on conforming levels only
+      if (mode == 4) fn = k_CD<K, 4, T, HG>;
+    }
     if (sm > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
       if (e != cudaSuccess) return e;
     }
-    fn<<<grid, th, sm, v.st>>>(dst, w, p, pfix, v.pfq, v.pff, cC, v.invd, v.mesh);
+    fn<<<grid, th, sm, v.st>>>(dst, w, p, pfix, v.pfq, v.pff, cC, v.invd, v.mesh, ch);
     return cudaGetLastError();
   };
-  // mode 3 (dst -= C w) is not idempotent: it uses the choice made for mode 0
-  const bool idem = mode != 3 && dst != w && dst != p && dst != pfix;
-  const int cpb = tuned_cpb(v.tune, v.st, TF_CD, K, mode == 3 ? 0 : mode, HG, (int)sizeof(T),
-                            v.nc, idem, launch);
+  // modes 3 (dst -= C w) and 4 (x += d) are not idempotent: they use the
+  // choices made for modes 0 and 1
+  const bool idem = mode < 3 && dst != w && dst != p && dst != pfix;
+  const int key = mode == 3 ? 0 : (mode == 4 ? 1 : mode);
+  const int cpb = tuned_cpb(v.tune, v.st, TF_CD, K, key, HG, (int)sizeof(T), v.nc, idem, launch);
   ATM_CUDA(launch(cpb));
   g_kernel_launches.fetch_add(1);
   return ATM_OK;

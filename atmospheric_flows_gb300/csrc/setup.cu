@@ -18,7 +18,10 @@ namespace atm {
 
 int upload_basis_rhs(const double *t);
 int upload_basis_impl(const double *t);
-int upload_basis_hang(const double *t);
+int upload_basis_hang_rho(const double *t);
+int upload_basis_hang_vel(const double *t);
+int upload_basis_hang_pres(const double *t);
+int upload_basis_hang_schur(const double *t);
 
 // Legendre P_n(x) and P_n'(x) by the three-term recurrence
 static void legendre_pd(int n, double x, double *p, double *dp) {
@@ -138,7 +141,8 @@ int upload_basis_all() {
     }
   }
   if (upload_basis_rhs(tab.data()) || upload_basis_impl(tab.data()) ||
-      upload_basis_hang(tab.data())) {
+      upload_basis_hang_rho(tab.data()) || upload_basis_hang_vel(tab.data()) ||
+      upload_basis_hang_pres(tab.data()) || upload_basis_hang_schur(tab.data())) {
     set_error("failed to upload basis tables to constant memory");
     return ATM_CUDA_ERROR;
   }
