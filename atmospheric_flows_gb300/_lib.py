@@ -66,6 +66,7 @@ SIGNATURES = {
     "atm_solver_set_state_device": (_i, [_h, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "atm_solver_get_state_device": (_i, [_h, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "atm_solver_set_sponge": (_i, [_h, _dp, _d, _d]),
+    "atm_solver_set_sponge_target": (_i, [_h, ctypes.c_void_p]),
     "atm_solver_set_clock": (_i, [_h, _d, ctypes.c_long]),
     "atm_solver_run": (_i, [_h, _i]),
     "atm_solver_stats": (_i, [_h, _dp]),

@@ -213,7 +213,7 @@ int vec_maxdiff(cudaStream_t st, const double *a, const double *b, long n, doubl
 int vec_diagnostics(cudaStream_t st, const double *rho, const double *u, const double *p,
                     int nc, int nn2, double *red, double *out);
 int vec_sponge(cudaStream_t st, double *u, const double *alpha, double dt, double ub0,
-               double ub1, int nc, int nn2);
+               double ub1, const double *target, int nc, int nn2);
 
 // ------------------------------------------------------------- MG levels --
 // Operator data of one multigrid level (T = float: mixed precision; double:
@@ -329,6 +329,7 @@ struct Solver {
   int last_picard[2] = {0, 0};
   double ubg0 = 0.0, ubg1 = 0.0;
   bool sponge = false;
+  double *sponge_target = nullptr;  // per-node target velocity, or the (ubg0, ubg1)
   // state and stage vectors (device)
   double *rho_old, *rho_tmp_2, *rho_tmp_3, *rho_curr, *rhs_rho;
   double *u_old, *u_tmp_2, *u_tmp_3, *u_curr, *u_fixed, *rhs_u, *tmp_1;

@@ -502,6 +502,20 @@ int atm_solver_set_sponge(atm_handle h, const double *alpha, double ubg_x, doubl
   v.ubg1 = ubg_z;
   return ATM_OK;
 }
+int atm_solver_set_sponge_target(atm_handle h, const double *u_target) {
+  CHECK_S(h);
+  Solver &v = *h->solver;
+  if (!u_target) {
+    cudaFree(v.sponge_target);
+    v.sponge_target = nullptr;
+    return ATM_OK;
+  }
+  const size_t n = h->n_vector() * sizeof(double);
+  if (!v.sponge_target) ATM_CUDA(cudaMalloc(&v.sponge_target, n));
+  ATM_CUDA(cudaMemcpyAsync(v.sponge_target, u_target, n, cudaMemcpyHostToDevice, h->stream));
+  ATM_CUDA(cudaStreamSynchronize(h->stream));
+  return ATM_OK;
+}
 int atm_solver_set_clock(atm_handle h, double time, long steps) {
   CHECK_S(h);
   if (steps < 0 || !(time >= 0.0)) { set_error("time and steps must be >= 0"); return ATM_BAD_ARG; }

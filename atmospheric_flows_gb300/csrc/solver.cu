@@ -38,7 +38,9 @@ int solver_alloc(atm_ctx &c, Solver &s) {
 
 void solver_free(Solver &s) {
   cudaFree(s.pool);
+  cudaFree(s.sponge_target);
   s.pool = nullptr;
+  s.sponge_target = nullptr;
 }
 
 namespace {
@@ -187,7 +189,8 @@ int solver_step(atm_ctx &c, Solver &s) {
   TRY(vec_copy(c.stream, s.rho_old, s.rho_curr, ns));
   TRY(vec_copy(c.stream, s.u_old, s.u_curr, nv));
   if (s.sponge)
-    TRY(vec_sponge(c.stream, s.u_old, s.alpha, c.dt, s.ubg0, s.ubg1, c.nc, c.nn2));
+    TRY(vec_sponge(c.stream, s.u_old, s.alpha, c.dt, s.ubg0, s.ubg1, s.sponge_target, c.nc,
+                   c.nn2));
   return ATM_OK;
 }
 

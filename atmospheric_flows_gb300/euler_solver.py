@@ -29,7 +29,10 @@ class EulerSolver:
     PRECISION_FP64_MG = 2  # FGMRES + FP64 multigrid V-cycle
 
     def __init__(self, case, eps=1e-8, max_its=None, precision=0, dt=None, mg_levels=8,
-                 true_residual_check=False, stream=None):
+                 true_residual_check=False, stream=None, levels=None, sponge_target=None):
+        """`levels`: precomputed multigrid levels (default: the hill hierarchy of
+        case.params); `sponge_target`: per-node sponge target velocity (batched
+        members with different background winds)."""
         # Krylov iteration cap per Schur solve: the reference's GMRES cap for
         # precision 0; multigrid-preconditioned FGMRES needs tens, so a solve
         # that stalls gives up after 1000 instead of running for minutes
@@ -46,7 +49,8 @@ class EulerSolver:
         if self.precision in (self.PRECISION_MIXED, self.PRECISION_FP64_MG):
             from .hill import mg_hierarchy
 
-            for level in mg_hierarchy(case.params, max_levels=mg_levels):
+            for level in (levels if levels is not None
+                          else mg_hierarchy(case.params, max_levels=mg_levels)):
                 self.op.add_mg_level(level)
         _lib.call("atm_solver_init", self.op.handle, self.dt, case.Ma, case.Fr, float(eps),
                   int(max_its), int(precision))
@@ -55,6 +59,11 @@ class EulerSolver:
         alpha = np.ascontiguousarray(case.sponge_alpha, dtype=np.float64)
         if np.any(alpha > 0):
             _lib.call("atm_solver_set_sponge", self.op.handle, _d(alpha), case.params.u0, 0.0)
+            if sponge_target is not None:
+                tgt = np.ascontiguousarray(sponge_target, dtype=np.float64)
+                if tgt.shape != (2 * self.n_scalar,):
+                    raise ValueError("sponge_target must hold 2 * n_scalar values")
+                _lib.call("atm_solver_set_sponge_target", self.op.handle, _d(tgt))
 
     def set_state(self, rho, u, p):
         r, uu, pp = (np.ascontiguousarray(a, dtype=np.float64) for a in (rho, u, p))

@@ -11,7 +11,12 @@ under continuous batching:
     members overlap on the device, and requests that arrive while others run
     join as soon as memory frees up;
   * members advance with the mixed-precision solver (FP64 state, FGMRES
-    with an FP32 multigrid preconditioner) unless told otherwise.
+    with an FP32 multigrid preconditioner) unless told otherwise;
+  * with batch_size > 1, requests waiting at admission that share mesh size,
+    degree and solver are concatenated into one context (batch.py): every
+    kernel launch then covers all of their cells.  A batch runs until its
+    longest member is done; each member's result is taken when its own step
+    count is reached.
 
 Members never share device data or reductions, so a member's result is the
 same alone and in a mix (the kernels are deterministic).  The reference has
@@ -28,6 +33,7 @@ import time
 import numpy as np
 
 from . import _lib
+from .batch import batch_key, concat
 from .hill import HillParams, build_case
 
 MESHES = ((40, 20), (80, 40), (160, 80), (320, 160))
@@ -103,11 +109,14 @@ def member_bytes(p: HillParams, precision: int = 1) -> int:
 class Server:
     """Continuous-batching scheduler for ensemble members on one GPU."""
 
-    def __init__(self, hbm_budget=150e9, max_running=32, chunk_steps=10, keep_state=False):
+    def __init__(self, hbm_budget=150e9, max_running=32, chunk_steps=10, keep_state=False,
+                 batch_size=1):
         self.budget = float(hbm_budget)
         self.max_running = int(max_running)
         self.chunk = int(chunk_steps)
         self.keep_state = keep_state
+        self.batch_size = int(batch_size)
+        self.batches = []  # member count of every batch started
         self._lock = threading.Condition()
         self._in_use = 0.0
         self._running = 0
@@ -155,39 +164,114 @@ class Server:
                                                  req.steps, dofs, status, state))
                 self._lock.notify_all()
 
+    def _run_batch(self, reqs, t0: float, nbytes: float):
+        from .euler_solver import EulerSolver
+
+        admitted = time.perf_counter() - t0
+        n = len(reqs)
+        finished = [None] * n
+        states = [None] * n
+        status = "ok"
+        stream = ctypes.c_void_p()
+        solver = None
+        dofs = [0] * n
+        try:
+            _lib.call("atm_stream_create", ctypes.byref(stream))
+            cases = [build_case(r.params) for r in reqs]
+            dofs = [c.n_dofs for c in cases]
+            b = concat(cases)
+            prec = reqs[0].precision
+            solver = EulerSolver(b.case, eps=reqs[0].eps, precision=prec,
+                                 true_residual_check=prec != 0, stream=stream.value,
+                                 levels=b.levels if prec != 0 else None,
+                                 sponge_target=b.u_target)
+            target = [r.steps for r in reqs]
+            steps = 0
+            while steps < max(target):
+                nxt = min(t for t in target if t > steps)
+                k = min(self.chunk, nxt - steps)
+                solver.run(k)
+                steps += k
+                due = [i for i in range(n) if finished[i] is None and target[i] <= steps]
+                if due:
+                    parts = b.split_state(solver.get_state()) if self.keep_state else None
+                    if parts is None:
+                        solver.diagnostics()  # one small read-back per result
+                    now = time.perf_counter() - t0
+                    for i in due:
+                        finished[i] = now
+                        if parts is not None:
+                            states[i] = tuple(np.array(a) for a in parts[i])
+        except Exception as exc:  # a failed batch must not stop the server
+            status = f"error: {exc}"
+        finally:
+            if solver is not None:
+                solver.close()
+            if stream.value:
+                _lib.call("atm_stream_destroy", stream)
+            end = time.perf_counter() - t0
+            with self._lock:
+                self._in_use -= nbytes
+                self._running -= 1
+                for i, r in enumerate(reqs):
+                    self.results.append(MemberResult(
+                        r.request_id, r.arrival, admitted,
+                        finished[i] if finished[i] is not None else end, r.steps, dofs[i],
+                        status, states[i]))
+                self._lock.notify_all()
+
     def run(self, requests, time_scale=1.0):
         """Serve `requests` (arrival times scaled by `time_scale`); returns
         the results ordered by request id."""
         _lib.load()
         pending = sorted(requests, key=lambda r: r.arrival)
+        queue = []  # arrived, not yet admitted (arrival order)
         threads = []
         t0 = time.perf_counter()
-        i = 0
         with self._lock:
-            while i < len(pending):
+            while pending or queue:
                 now = time.perf_counter() - t0
-                req = pending[i]
-                due = req.arrival * time_scale
-                if due > now:
-                    self._lock.wait(timeout=due - now)
+                while pending and pending[0].arrival * time_scale <= now:
+                    queue.append(pending.pop(0))
+                if not queue:
+                    self._lock.wait(timeout=pending[0].arrival * time_scale - now)
                     continue
-                nb = member_bytes(req.params, req.precision)
-                if nb > self.budget:
-                    self.results.append(MemberResult(req.request_id, req.arrival, now, now,
-                                                     req.steps, 0, "rejected: over budget"))
-                    i += 1
+                head = queue[0]
+                if member_bytes(head.params, head.precision) > self.budget:
+                    queue.pop(0)
+                    self.results.append(MemberResult(head.request_id, head.arrival, now, now,
+                                                     head.steps, 0, "rejected: over budget"))
                     continue
+                group = [head]
+                if self.batch_size > 1:
+                    key = (batch_key(head.params), head.precision, head.eps)
+                    for r in queue[1:]:
+                        if len(group) >= self.batch_size:
+                            break
+                        if (batch_key(r.params), r.precision, r.eps) == key:
+                            group.append(r)
+                nb = sum(member_bytes(r.params, r.precision) for r in group)
+                while len(group) > 1 and nb > self.budget:
+                    group.pop()
+                    nb = sum(member_bytes(r.params, r.precision) for r in group)
                 if self._in_use + nb > self.budget or self._running >= self.max_running:
                     self._lock.wait(timeout=0.05)
                     continue
+                for r in group:
+                    queue.remove(r)
                 self._in_use += nb
                 self._running += 1
                 self.peak_running = max(self.peak_running, self._running)
                 self.peak_bytes = max(self.peak_bytes, self._in_use)
-                th = threading.Thread(target=self._run_member, args=(req, t0, nb), daemon=True)
+                self.batches.append(len(group))
+                if len(group) == 1:
+                    th = threading.Thread(target=self._run_member, args=(head, t0, nb),
+                                          daemon=True)
+                else:
+                    th = threading.Thread(target=self._run_batch, args=(group, t0, nb),
+                                          daemon=True)
                 th.start()
                 threads.append(th)
-                i += 1
         for th in threads:
             th.join()
         self.makespan = time.perf_counter() - t0

@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--serving-compare", action="store_true",
                     help="serve one ensemble with FP64 and with mixed-precision multigrid "
                          "and compare throughput and fields")
+    ap.add_argument("--serving-batch", type=int, default=1,
+                    help="concatenate up to this many waiting same-mesh members per context")
     ap.add_argument("--serving-requests", type=int, default=48)
     ap.add_argument("--serving-rate", type=float, default=8.0)
     ap.add_argument("--serving-steps-scale", type=float, default=0.05)
@@ -453,10 +455,12 @@ def serving(args):
 
     reqs = make_requests(n=args.serving_requests, rate=args.serving_rate, seed=0,
                          steps_scale=args.serving_steps_scale)
-    srv = Server(hbm_budget=150e9, max_running=32)
+    srv = Server(hbm_budget=150e9, max_running=32, batch_size=args.serving_batch)
     res = srv.run(reqs)
     s = summarize(res, srv.makespan)
     s.update({"metric": "ensemble serving latency / aggregate DoF-steps/s", "unit": "s",
+              "batch_size": args.serving_batch, "batches": len(srv.batches),
+              "members_per_batch_mean": float(np.mean(srv.batches)) if srv.batches else 0.0,
               "requests_sample": f"{args.serving_requests} requests, Poisson rate "
                                  f"{args.serving_rate}/s, steps 100-400 scaled by "
                                  f"{args.serving_steps_scale}, meshes 40x20..320x160, k 2-5",

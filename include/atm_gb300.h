@@ -247,6 +247,11 @@ int atm_solver_set_state_device(atm_handle h, const double *rho, const double *u
 int atm_solver_get_state_device(atm_handle h, double *rho, double *u, double *p);
 int atm_solver_set_sponge(atm_handle h, const double *alpha_nodes, double ubg_x,
                           double ubg_z);
+/* Per-node target velocity of the sponge ([cell][2][node], host, 2*n_scalar
+ * values) instead of the constant (ubg_x, ubg_z); NULL returns to the
+ * constant.  Lets one context hold several flow-over-hill members with
+ * different background winds (batched serving).  No reference counterpart. */
+int atm_solver_set_sponge_target(atm_handle h, const double *u_target);
 /* Restore the simulated time and step count (checkpoint restart). */
 int atm_solver_set_clock(atm_handle h, double time, long steps);
 int atm_solver_run(atm_handle h, int n_steps);

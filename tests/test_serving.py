@@ -59,3 +59,68 @@ def test_server_budget_and_latency(cuda_ok):
     assert srv.peak_bytes <= budget
     assert s["p50_latency_s"] <= s["p95_latency_s"] <= s["p99_latency_s"]
     assert s["aggregate_dof_steps_per_s"] > 0
+
+
+def _batch_cases():
+    from atmospheric_flows_gb300.hill import build_case
+
+    return [build_case(HillParams(nx=16, nz=8, degree=3, h0=h, u0=u, seed=s, theta_noise=0.1))
+            for h, u, s in ((300.0, 8.0, 1), (450.0, 12.0, 2), (200.0, 6.0, 3))]
+
+
+def test_batch_tables_are_block_diagonal():
+    from atmospheric_flows_gb300 import batch
+
+    cases = _batch_cases()
+    b = batch.concat(cases)
+    nc = cases[0].n_cells
+    assert b.case.n_cells == 3 * nc and b.offsets == [0, nc, 2 * nc]
+    assert b.case.dt == min(c.dt for c in cases)
+    member = lambda cell: cell // nc  # noqa: E731
+    inner = b.case.inner_faces
+    assert np.all(member(inner[:, 0]) == member(inner[:, 2]))
+    assert len(inner) == 3 * len(cases[0].inner_faces)
+    assert len(b.case.boundary_faces) == 3 * len(cases[0].boundary_faces)
+    prev = nc
+    for lv in b.levels:
+        m = lv["n_cells"] // 3
+        ch = lv["children"]
+        assert sorted(ch.ravel().tolist()) == list(range(3 * prev))
+        assert np.all(ch // prev == (np.arange(3 * m) // m)[:, None])
+        prev = m
+    tgt = b.u_target.reshape(3 * nc, 2, -1)
+    assert np.all(tgt[:nc, 0] == 8.0) and np.all(tgt[nc:2 * nc, 0] == 12.0)
+    assert np.all(tgt[:, 1] == 0.0)
+    rho = b.split(b.case.rho)
+    assert all(np.array_equal(r, c.rho) for r, c in zip(rho, cases))
+
+
+@pytest.mark.gpu
+def test_member_same_alone_and_in_batch(cuda_ok):
+    from atmospheric_flows_gb300 import batch
+    from atmospheric_flows_gb300.euler_solver import EulerSolver
+
+    cases = _batch_cases()
+    b = batch.concat(cases)
+    kw = dict(eps=1e-10, precision=1, true_residual_check=True)
+    g = EulerSolver(b.case, levels=b.levels, sponge_target=b.u_target, **kw)
+    g.run(3)
+    parts = b.split_state(g.get_state())
+    g.close()
+    for i, c in enumerate(cases):
+        s = EulerSolver(c, dt=b.case.dt, **kw)
+        s.run(3)
+        for a, ref in zip(parts[i], s.get_state()):
+            assert np.linalg.norm(a - ref) / np.linalg.norm(ref) < 1e-8
+        s.close()
+
+
+@pytest.mark.gpu
+def test_server_forms_batches(cuda_ok):
+    reqs = make_requests(n=8, rate=200.0, seed=9, meshes=((40, 20),), degrees=(2,),
+                         steps_range=(2, 5))
+    srv = Server(batch_size=4)
+    res = srv.run(reqs)
+    s = summarize(res, srv.makespan)
+    assert s["completed"] == 8, s
+    assert max(srv.batches) > 1 and sum(srv.batches) == 8
