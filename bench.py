@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--serving-batch", type=int, default=1,
                     help="concatenate up to this many waiting same-mesh members per context")
     ap.add_argument("--serving-requests", type=int, default=48)
+    ap.add_argument("--serving-meshes", default="40x20,80x40,160x80,320x160")
+    ap.add_argument("--serving-degrees", default="2,3,4,5")
     ap.add_argument("--serving-rate", type=float, default=8.0)
     ap.add_argument("--serving-steps-scale", type=float, default=0.05)
     ap.add_argument("--amr", action="store_true",
@@ -453,8 +455,10 @@ def serving(args):
     torch.cuda.set_device(0)
     from atmospheric_flows_gb300.serving import Server, make_requests, summarize
 
+    meshes = tuple(tuple(int(v) for v in m.split("x")) for m in args.serving_meshes.split(","))
+    degrees = tuple(int(k) for k in args.serving_degrees.split(","))
     reqs = make_requests(n=args.serving_requests, rate=args.serving_rate, seed=0,
-                         steps_scale=args.serving_steps_scale)
+                         steps_scale=args.serving_steps_scale, meshes=meshes, degrees=degrees)
     srv = Server(hbm_budget=150e9, max_running=32, batch_size=args.serving_batch)
     res = srv.run(reqs)
     s = summarize(res, srv.makespan)
@@ -463,7 +467,8 @@ def serving(args):
               "members_per_batch_mean": float(np.mean(srv.batches)) if srv.batches else 0.0,
               "requests_sample": f"{args.serving_requests} requests, Poisson rate "
                                  f"{args.serving_rate}/s, steps 100-400 scaled by "
-                                 f"{args.serving_steps_scale}, meshes 40x20..320x160, k 2-5",
+                                 f"{args.serving_steps_scale}, meshes {args.serving_meshes}, "
+                                 f"k {args.serving_degrees}",
               "hbm_budget_gb": 150, "peak_running": srv.peak_running,
               "peak_reserved_gb": srv.peak_bytes / 1e9,
               "solver": "FP64 state, FGMRES + FP32 multigrid, rtol 1e-8 true residual"})
