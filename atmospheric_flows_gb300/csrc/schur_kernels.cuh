@@ -102,11 +102,24 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
       const T *b0 = bt + (lc * 2 + 0) * NN2, *b1 = bt + (lc * 2 + 1) * NN2;
       for (int i = col; i < NN2; i += NQ) {
         T s0 = T(0.0), s1 = T(0.0);
+        if constexpr (sizeof(T) == 4) {
+          // FP32 (multigrid levels): latency bound, so all NN2 loads of the
+          // A^{-1} column go out before the FMAs
+          T a[NN2];
+#pragma unroll
+          for (int j = 0; j < NN2; ++j) a[j] = Ab[j * NN2 + i];  // transposed storage
+#pragma unroll
+          for (int j = 0; j < NN2; ++j) {
+            s0 = fma(a[j], b0[j], s0);
+            s1 = fma(a[j], b1[j], s1);
+          }
+        } else {
 #pragma unroll 5
-        for (int j = 0; j < NN2; ++j) {
-          const T a = Ab[j * NN2 + i];  // transposed storage
-          s0 = fma(a, b0[j], s0);
-          s1 = fma(a, b1[j], s1);
+          for (int j = 0; j < NN2; ++j) {
+            const T a = Ab[j * NN2 + i];  // transposed storage
+            s0 = fma(a, b0[j], s0);
+            s1 = fma(a, b1[j], s1);
+          }
         }
         dst[((long)c * 2 + 0) * NN2 + i] = s0;
         dst[((long)c * 2 + 1) * NN2 + i] = s1;
