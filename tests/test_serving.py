@@ -127,3 +127,64 @@ def test_server_forms_batches(cuda_ok):
     s = summarize(res, srv.makespan)
     assert s["completed"] == 8, s
     assert max(srv.batches) > 1 and sum(srv.batches) == 8
+
+
+class _FakeServer(Server):
+    """Scheduler under test with the device work replaced by a short sleep."""
+
+    def __init__(self, **kw):
+        super().__init__(**kw)
+        self.groups = []
+        self.max_seen = 0
+
+    def _finish(self, reqs, t0, nbytes):
+        import time as _t
+
+        from atmospheric_flows_gb300.serving import MemberResult
+
+        with self._lock:
+            self.max_seen = max(self.max_seen, self._running)
+        _t.sleep(0.02)
+        now = _t.perf_counter() - t0
+        with self._lock:
+            self._in_use -= nbytes
+            self._running -= 1
+            for r in reqs:
+                self.results.append(MemberResult(r.request_id, r.arrival, now, now, r.steps, 1,
+                                                 "ok"))
+            self._lock.notify_all()
+
+    def _run_member(self, req, t0, nbytes):
+        self.groups.append([req.request_id])
+        self._finish([req], t0, nbytes)
+
+    def _run_batch(self, reqs, t0, nbytes):
+        self.groups.append([r.request_id for r in reqs])
+        self._finish(reqs, t0, nbytes)
+
+
+def test_scheduler_budget_batching_and_limits():
+    small = dict(meshes=((40, 20),), degrees=(2,))
+    reqs = make_requests(n=20, rate=1e6, seed=4, **small)  # all arrive at once
+    big = MemberRequest(99, 0.0, HillParams(nx=320, nz=160, degree=5), 10)
+    budget = 6 * member_bytes(reqs[0].params)
+    srv = _FakeServer(hbm_budget=budget, max_running=3, batch_size=4)
+    res = srv.run(reqs + [big])
+    by_id = {r.request_id: r for r in res}
+    assert by_id[99].status.startswith("rejected")
+    assert all(by_id[r.request_id].status == "ok" for r in reqs)
+    # same key: groups of up to 4, never more than 3 contexts at once, budget kept
+    assert max(len(g) for g in srv.groups) == 4
+    assert sorted(i for g in srv.groups for i in g) == sorted(r.request_id for r in reqs)
+    assert srv.max_seen <= 3 and srv.peak_bytes <= budget
+
+
+def test_scheduler_does_not_mix_keys():
+    a = make_requests(n=6, rate=1e6, seed=5, meshes=((40, 20),), degrees=(2,))
+    b = make_requests(n=6, rate=1e6, seed=6, meshes=((40, 20),), degrees=(3,))
+    for i, r in enumerate(b):
+        r.request_id = 100 + i
+    srv = _FakeServer(batch_size=8)
+    srv.run(a + b)
+    for g in srv.groups:
+        assert all(i < 100 for i in g) or all(i >= 100 for i in g)
