@@ -68,11 +68,15 @@ int atm_ctx_create(int dim, int degree, int n_cells, int mapping_degree,
                    int n_bdry, const int *bdry_faces, atm_handle *out);
 int atm_ctx_destroy(atm_handle h);
 /* Re-upload geometry and connectivity after mesh adaptation (same sizes).
- * Drops the multigrid levels: add them again for the new mesh. */
+ * Drops the multigrid levels: add them again for the new mesh.  Replaces the
+ * MatrixFree::reinit that follows a refinement (Atmospheric_Flow.cc:283,
+ * 325-348). */
 int atm_upload_mesh(atm_handle h, int mapping_degree, const double *mapping_nodes,
                     int n_inner, const int *inner_faces, int n_bdry,
                     const int *bdry_faces);
-/* cudaStream_t as void*; NULL = the legacy default stream. */
+/* cudaStream_t as void*; NULL = the legacy default stream.  Streams, device
+ * memory queries and the FMA probe below have no reference counterpart
+ * (deal.II runs on the host). */
 int atm_set_stream(atm_handle h, void *stream);
 int atm_synchronize(atm_handle h);
 /* A non-blocking CUDA stream (as void*) for one member of an ensemble, so
@@ -82,7 +86,8 @@ int atm_stream_create(void **out);
 int atm_stream_destroy(void *stream);
 /* cudaMemGetInfo of the current device, for admission against a budget. */
 int atm_device_memory(double *free_bytes, double *total_bytes);
-/* Sizes: scalar field length n_cells*(k+1)^2; velocity twice that. */
+/* Sizes: scalar field length n_cells*(k+1)^2; velocity twice that (the
+ * DoFHandler sizes written at Atmospheric_Flow.cc:250-252). */
 long atm_n_scalar(atm_handle h);
 
 /* Instrumentation (replaces deal.II TimerOutput, Atmospheric_Flow.cc:176-178,
@@ -187,11 +192,13 @@ int atm_mg_add_level(atm_handle h, int n_cells, int mapping_degree, const double
                      int n_inner, const int *inner_faces, int n_bdry, const int *bdry_faces,
                      const int *children);
 /* Chebyshev degree (3), smoothing range (15), power iterations for the
- * largest eigenvalue (10), degree of the coarsest-level Chebyshev (20). */
+ * largest eigenvalue (10), degree of the coarsest-level Chebyshev (20).
+ * Replaces the smoother_data set-up of Atmospheric_Flow.cc:477-498,594-615. */
 int atm_mg_set_smoother(atm_handle h, int degree, double smoothing_range, int eig_iterations,
                         int coarse_degree);
 /* One V-cycle: dst ~= S^{-1} src (FP64 device vectors); precision 1 runs the
- * V-cycle in FP32, 2 in FP64. */
+ * V-cycle in FP32, 2 in FP64.  Replaces PreconditionMG::vmult
+ * (Atmospheric_Flow.cc:518-522, 635-642), here on the Schur operator. */
 int atm_mg_vcycle(atm_handle h, int precision, double *dst, const double *src);
 /* Replay the V-cycle as a captured CUDA graph (1, default) or launch its
  * kernels one by one (0).  Same kernels, same arguments, same results; the
@@ -199,7 +206,8 @@ int atm_mg_vcycle(atm_handle h, int precision, double *dst, const double *src);
  * eigenvalue estimates change.  No reference counterpart (deal.II's
  * PreconditionMG::vmult, Atmospheric_Flow.cc:517-536, runs on the host). */
 int atm_mg_set_graphs(atm_handle h, int on);
-/* out[0] = V-cycles run, out[1] = of those, replays of a captured graph. */
+/* out[0] = V-cycles run, out[1] = of those, replays of a captured graph.
+ * No reference counterpart. */
 int atm_mg_stats(atm_handle h, long *out);
 
 /* Tile-shape autotuner of the face kernels (the explicit right-hand sides, B
@@ -215,7 +223,9 @@ int atm_set_autotune(atm_handle h, int on);
  * cells per block).  Returns the number of entries (may exceed max_entries). */
 int atm_autotune_table(int *out, int max_entries);
 /* FGMRES(16) + V-cycle on S x = b (NS 2 operator state); tol absolute on the
- * unpreconditioned residual; precision as for atm_mg_vcycle. */
+ * unpreconditioned residual; precision as for atm_mg_vcycle.  Replaces the
+ * Schur GMRES of Atmospheric_Flow.cc:657-672 with a multigrid-preconditioned
+ * flexible GMRES. */
 int atm_solve_fgmres(atm_handle h, int precision, double *x, const double *b, double tol,
                      int maxit, int *iters, double *res);
 /* S is not linear (the upwind lambda of C depends on A^{-1}B p,
@@ -245,6 +255,10 @@ int atm_solver_get_state(atm_handle h, double *rho, double *u, double *p);
 int atm_solver_set_state_device(atm_handle h, const double *rho, const double *u,
                                 const double *p);
 int atm_solver_get_state_device(atm_handle h, double *rho, double *u, double *p);
+/* Rayleigh sponge: after each step relax u toward (ubg_x, ubg_z) with rate
+ * alpha_nodes (1/s per node; NULL switches it off).  Not in the reference: it
+ * is the flow-over-hill absorbing layer, applied where the reference's step
+ * ends (Atmospheric_Flow.cc:1220-1222). */
 int atm_solver_set_sponge(atm_handle h, const double *alpha_nodes, double ubg_x,
                           double ubg_z);
 /* Per-node target velocity of the sponge ([cell][2][node], host, 2*n_scalar
@@ -252,7 +266,9 @@ int atm_solver_set_sponge(atm_handle h, const double *alpha_nodes, double ubg_x,
  * constant.  Lets one context hold several flow-over-hill members with
  * different background winds (batched serving).  No reference counterpart. */
 int atm_solver_set_sponge_target(atm_handle h, const double *u_target);
-/* Restore the simulated time and step count (checkpoint restart). */
+/* Restore the simulated time and step count (checkpoint restart).  No
+ * reference counterpart (the reference writes VTU output only,
+ * Atmospheric_Flow.cc:885-918). */
 int atm_solver_set_clock(atm_handle h, double time, long steps);
 int atm_solver_run(atm_handle h, int n_steps);
 /* stats[0..8] as doubles: steps, Picard iterations (total), Krylov
