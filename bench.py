@@ -480,9 +480,11 @@ def serving(args):
 
 def serving_sweep(args):
     """The serving sample at several Poisson rates: p50/p95/p99 latency, mean
-    queue wait and aggregate throughput per rate.  The sustained rate is the
-    highest rate whose mean queue wait stays under 1 s, i.e. at which
-    admission keeps up with arrivals; its p99 is the headline latency."""
+    queue wait and aggregate throughput per rate.  A rate is sustained when
+    the server drains: its makespan ends within the lowest rate's p99 latency
+    after the last arrival (admission never backs up here, so a backlog
+    shows as members slowed by sharing the GPU).  The p99 at the highest
+    sustained rate is the headline latency."""
     import torch
 
     torch.cuda.set_device(0)
@@ -498,10 +500,14 @@ def serving_sweep(args):
         srv = Server(hbm_budget=150e9, max_running=32, batch_size=args.serving_batch)
         res = srv.run(reqs)
         s = summarize(res, srv.makespan)
-        rows.append({"rate_per_s": rate, **{k: s[k] for k in (
+        last = max(r.arrival for r in reqs)
+        rows.append({"rate_per_s": rate, "last_arrival_s": last, **{k: s[k] for k in (
             "completed", "p50_latency_s", "p95_latency_s", "p99_latency_s", "mean_queue_wait_s",
             "aggregate_dof_steps_per_s", "makespan_s")}})
-    kept = [r for r in rows if r["mean_queue_wait_s"] < 1.0 and r["completed"] == args.serving_requests]
+    rows.sort(key=lambda r: r["rate_per_s"])
+    ref_p99 = rows[0]["p99_latency_s"]
+    kept = [r for r in rows if r["completed"] == args.serving_requests
+            and r["makespan_s"] - r["last_arrival_s"] <= ref_p99]
     sustained = max(kept, key=lambda r: r["rate_per_s"]) if kept else None
     print(json.dumps({
         "metric": "ensemble serving latency by request rate", "unit": "s",
@@ -512,7 +518,8 @@ def serving_sweep(args):
                   f"{args.serving_steps_scale}, meshes {args.serving_meshes}, k "
                   f"{args.serving_degrees}, mixed-precision solver rtol 1e-8, HBM budget "
                   f"150 GB, batch size {args.serving_batch}",
-        "sustained_rule": "highest rate with mean queue wait < 1 s and every request done"}),
+        "sustained_rule": "highest rate whose makespan ends within the lowest rate's p99 "
+                          "after the last arrival, every request done"}),
           flush=True)
     return 0
 
