@@ -215,3 +215,36 @@ def test_indicator_and_marking():
     refined = {iz * p.nx + ix for (l, ix, iz) in t1.refined if l == 0}
     assert refined == set(np.nonzero(ind > np.quantile(ind, 0.9))[0].tolist())
     assert len(t1.leaves()) == p.nx * p.nz + 3 * len(refined)
+
+
+@pytest.mark.parametrize("k", [1, 2, 4, 5])
+def test_oracle_hanging_identities_all_degrees(k):
+    """Mass conservation of the rho rhs, the rest states and the B/C
+    integration by parts on 2:1 meshes, for every supported degree."""
+    p = HillParams(nx=5, nz=3, degree=k, cfl=2.0)
+    case = amr.adaptive_case(p, amr.example_tree(p.nx, p.nz))
+    op = OracleOperator(case)
+    rho, u, pr = perturbed(case, seed=k)
+    for stage in (1, 2, 3):
+        op.set_stage(stage, 1)
+        src = []
+        for j in range(stage):
+            src += [rho * (1 + 0.1 * j), u * (1 - 0.2 * j)]
+        r = op.vmult_rhs_rho_update(src)
+        m = op.vmult(rho)
+        assert abs(r.sum() - m.sum()) / abs(m.sum()) < 1e-13
+    z = np.zeros(2 * op.n_scalar)
+    op.set_stage(1, 6)
+    assert rel(op.vmult_rhs_pressure([rho, z, pr, rho, z]), op.vmult(pr)) < 1e-13
+    flat = HillParams(nx=5, nz=3, degree=k, h0=0.0, cfl=1.0)
+    fc = amr.adaptive_case(flat, amr.example_tree(flat.nx, flat.nz))
+    of = OracleOperator(fc)
+    n = of.n_scalar
+    of.set_pres_fixed(np.full(n, 0.9))
+    of.set_stage(1, 2)
+    rng = np.random.default_rng(k)
+    q = rng.standard_normal(n)
+    w = rng.standard_normal(2 * n)
+    lhs = np.dot(of.vmult_pressure(q), w) * fc.Ma ** 2
+    rhs = -np.dot(of.vmult_enthalpy(w), q) / (1.4 / 0.4 * 0.9)
+    assert abs(lhs - rhs) / abs(lhs) < 1e-11
