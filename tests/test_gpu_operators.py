@@ -50,6 +50,7 @@ CASES = [
     dict(nx=5, nz=3, degree=2, amr=True),
     dict(nx=4, nz=3, degree=4, periodic=False, amr=True),
     dict(nx=4, nz=2, degree=1, amr=True),
+    dict(nx=3, nz=2, degree=5, amr=True),
 ]
 
 
