@@ -22,6 +22,8 @@ SIGNATURES = {
     "atm_last_error": (ctypes.c_char_p, []),
     "atm_version": (ctypes.c_char_p, []),
     "atm_ctx_create": (_i, [_i, _i, _i, _i, _dp, _i, _ip, _i, _ip, ctypes.POINTER(_h)]),
+    "atm_check_mesh": (_i, [_i, _i, _i, ctypes.c_void_p, _i, ctypes.c_void_p, _i,
+                           ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "atm_ctx_destroy": (_i, [_h]),
     "atm_upload_mesh": (_i, [_h, _i, _dp, _i, _ip, _i, _ip]),
     "atm_set_stream": (_i, [_h, ctypes.c_void_p]),

@@ -94,6 +94,18 @@ static void ctx_free(atm_ctx *c) {
   delete c;
 }
 
+int atm_check_mesh(int degree, int n_cells, int mapping_degree, const double *mapping_nodes,
+                   int n_inner, const int *inner_faces, int n_bdry, const int *bdry_faces,
+                   int *n_hanging) {
+  if (degree < 1 || degree > KMAX) { set_error("degree must be in 1..5"); return ATM_BAD_ARG; }
+  if (n_cells < 1 || n_inner < 0 || n_bdry < 0) { set_error("bad sizes"); return ATM_BAD_ARG; }
+  HostMesh hm;
+  const int rc = build_mesh_tables(degree, n_cells, mapping_degree, mapping_nodes, n_inner,
+                                   inner_faces, n_bdry, bdry_faces, hm);
+  if (rc == ATM_OK && n_hanging) *n_hanging = hm.nhang;
+  return rc;
+}
+
 int atm_ctx_create(int dim, int degree, int n_cells, int mapping_degree,
                    const double *mapping_nodes, int n_inner, const int *inner_faces,
                    int n_bdry, const int *bdry_faces, atm_handle *out) {

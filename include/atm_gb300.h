@@ -67,6 +67,15 @@ int atm_ctx_create(int dim, int degree, int n_cells, int mapping_degree,
                    const double *mapping_nodes, int n_inner, const int *inner_faces,
                    int n_bdry, const int *bdry_faces, atm_handle *out);
 int atm_ctx_destroy(atm_handle h);
+/* Validate mesh tables on the host without a device (the checks
+ * atm_ctx_create makes): index ranges, opposite face pairs, every cell face
+ * listed once (a coarse hanging face twice, by its two subfaces), positive
+ * Jacobians.  On success *n_hanging (if given) is the number of hanging faces.
+ * Error messages as atm_ctx_create.  No reference counterpart (deal.II
+ * asserts on its own triangulation). */
+int atm_check_mesh(int degree, int n_cells, int mapping_degree, const double *mapping_nodes,
+                   int n_inner, const int *inner_faces, int n_bdry, const int *bdry_faces,
+                   int *n_hanging);
 /* Re-upload geometry and connectivity after mesh adaptation (same sizes).
  * Drops the multigrid levels: add them again for the new mesh.  Replaces the
  * MatrixFree::reinit that follows a refinement (Atmospheric_Flow.cc:283,
