@@ -194,3 +194,25 @@ def test_golden_fixture_regression():
     for name, v in (("rho", rho), ("u", u), ("p", p)):
         ref = g[name]
         assert np.linalg.norm(v - ref) / np.linalg.norm(ref) < 1e-11, name
+
+
+def test_golden_fixture_regression_adaptive():
+    """The oracle on a 2:1 adaptive mesh reproduces its fixture
+    (tests/golden/make_golden.py)."""
+    path = os.path.join(GOLDEN, "oracle_amr_k2.npz")
+    if not os.path.exists(path):
+        pytest.skip("golden fixture not generated")
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("make_golden",
+                                                  os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    g = np.load(path)
+    cfg = {k: g[k].item() for k in mg.AMR_CFG}
+    case = mg.amr_case(cfg)
+    s = OracleSolver(case, eps=cfg["eps"], inner_tol=cfg["inner_tol"])
+    s.run(int(cfg["steps"]))
+    for name, v in zip(("rho", "u", "p"), s.get_state()):
+        ref = g[name]
+        assert np.linalg.norm(v - ref) / np.linalg.norm(ref) < 1e-11, name
