@@ -3,7 +3,7 @@
 Bars: a V-cycle reduces the Schur residual; FGMRES+MG needs far fewer
 iterations than GMRES+Jacobi; N IMEX steps with the mixed-precision solve
 (rtol 1e-10) stay within 1e-8 relative L2 per field of the FP64 oracle (the
-spec bound for the mixed path); the FP64-multigrid path stays within
+parity bound for the mixed path); the FP64-multigrid path stays within
 1e-10.  S is not linear, so all sides solve the Schur equation to its true
 residual (the true-residual check) for these comparisons.
 """

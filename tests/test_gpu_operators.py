@@ -1,7 +1,7 @@
 """Single-operator parity: sm_103a kernels (through the C ABI) vs the FP64 oracle.
 
 Tolerance (single operator application): 1e-12 relative in the max norm,
-the spec bar for one vmult.  Schur applies and solves compare at the
+the parity bar for one vmult.  Schur applies and solves compare at the
 solver tolerance they are run to.
 """
 import numpy as np

@@ -1,6 +1,6 @@
 """Time-loop parity: N IMEX steps on the GB300 vs N steps of the FP64 oracle.
 
-Tolerance: 1e-10 relative L2 per field after N steps (the spec bar for
+Tolerance: 1e-10 relative L2 per field after N steps (the parity bar for
 the plain FP64 path).  Both sides run with tightened, identical solver
 tolerances so the comparison measures arithmetic, not stopping points.
 """
