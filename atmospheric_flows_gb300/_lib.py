@@ -71,6 +71,7 @@ SIGNATURES = {
     "atm_solver_set_sponge_target": (_i, [_h, ctypes.c_void_p]),
     "atm_solver_set_clock": (_i, [_h, _d, ctypes.c_long]),
     "atm_solver_run": (_i, [_h, _i]),
+    "atm_solver_set_continue_on_not_converged": (_i, [_h, _i]),
     "atm_solver_stats": (_i, [_h, _dp]),
     "atm_solver_diagnostics": (_i, [_h, _dp]),
 }

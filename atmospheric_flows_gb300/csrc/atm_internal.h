@@ -324,6 +324,10 @@ struct Solver {
   double eps = 1e-8;
   int max_its = 30000;
   int precision = 0;
+  // false (default): a Schur solve that reaches max_its ends the step with
+  // ATM_NOT_CONVERGED, as deal.II's SolverControl throws (caught in main,
+  // Atmospheric_Flow.cc:1289-1311); true: count it and carry on
+  bool continue_on_not_converged = false;
   double time = 0.0;
   long steps = 0, picard_total = 0, krylov_total = 0, failures = 0;
   int last_picard[2] = {0, 0};

@@ -535,6 +535,11 @@ int atm_solver_set_clock(atm_handle h, double time, long steps) {
   h->solver->steps = steps;
   return ATM_OK;
 }
+int atm_solver_set_continue_on_not_converged(atm_handle h, int on) {
+  CHECK_S(h);
+  h->solver->continue_on_not_converged = on != 0;
+  return ATM_OK;
+}
 int atm_solver_run(atm_handle h, int n_steps) {
   CHECK_S(h);
   if (n_steps < 0) { set_error("n_steps must be >= 0"); return ATM_BAD_ARG; }

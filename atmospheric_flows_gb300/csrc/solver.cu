@@ -13,6 +13,7 @@
 //     printouts in the reference, Atmospheric_Flow.cc:1121-1122,1225-1242);
 //     atm_solver_diagnostics computes them on demand.
 #include <cmath>
+#include <cstdio>
 
 #include "atm_device.cuh"
 
@@ -106,7 +107,17 @@ int pressure_fixed_point(atm_ctx &c, Solver &s) {
                ? gmres_schur(c, s.pres_fixed, s.rhs_pres, tol, s.max_its, &its, &res)
                : fgmres_mg(c, s.precision, s.pres_fixed, s.rhs_pres, tol, s.max_its, &its, &res);
   s.krylov_total += its;
-  if (rc == ATM_NOT_CONVERGED) { ++s.failures; rc = ATM_OK; }
+  if (rc == ATM_NOT_CONVERGED) {
+    ++s.failures;
+    if (s.continue_on_not_converged) return ATM_OK;
+    char msg[256];
+    std::snprintf(msg, sizeof msg,
+                  "Schur solve did not converge in IMEX stage %d of step %ld: %d iterations, "
+                  "residual %.3e > tolerance %.3e (step abandoned; the state is that of the "
+                  "last completed step)",
+                  c.hstage, s.steps + 1, its, res, tol);
+    set_error(msg);
+  }
   return rc;
 }
 
@@ -157,11 +168,12 @@ int picard(atm_ctx &c, Solver &s, int which) {
 
 }  // namespace
 
-// one pass of the while loop of Atmospheric_Flow.cc:1110-1250
+// one pass of the while loop of Atmospheric_Flow.cc:1110-1250.  The state
+// (rho_old, u_old, pres_old) is written only in stage 3, which has no Krylov
+// solve, so a step that fails in stage 1 or 2 leaves the state, the time and
+// the step count of the last completed step.
 int solver_step(atm_ctx &c, Solver &s) {
   const long ns = c.n_scalar(), nv = c.n_vector();
-  s.time += c.dt;
-  ++s.steps;
   // stage 1
   c.hstage = 1;
   TRY(update_density(c, s));
@@ -191,6 +203,8 @@ int solver_step(atm_ctx &c, Solver &s) {
   if (s.sponge)
     TRY(vec_sponge(c.stream, s.u_old, s.alpha, c.dt, s.ubg0, s.ubg1, s.sponge_target, c.nc,
                    c.nn2));
+  s.time += c.dt;
+  ++s.steps;
   return ATM_OK;
 }
 

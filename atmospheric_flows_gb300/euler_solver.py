@@ -29,10 +29,17 @@ class EulerSolver:
     PRECISION_FP64_MG = 2  # FGMRES + FP64 multigrid V-cycle
 
     def __init__(self, case, eps=1e-8, max_its=None, precision=0, dt=None, mg_levels=8,
-                 true_residual_check=False, stream=None, levels=None, sponge_target=None):
+                 true_residual_check=False, stream=None, levels=None, sponge_target=None,
+                 continue_on_not_converged=False):
         """`levels`: precomputed multigrid levels (default: the hill hierarchy of
         case.params); `sponge_target`: per-node sponge target velocity (batched
-        members with different background winds)."""
+        members with different background winds).
+
+        A Schur solve that reaches `max_its` makes :meth:`run` raise
+        ``AtmError`` (code NOT_CONVERGED) and leaves the state of the last
+        completed step, as the reference's SolverControl throws
+        (Atmospheric_Flow.cc:1289-1311); `continue_on_not_converged=True`
+        counts it in ``stats()["solve_fail"]`` and carries on instead."""
         # Krylov iteration cap per Schur solve: the reference's GMRES cap for
         # precision 0; multigrid-preconditioned FGMRES needs tens, so a solve
         # that stalls gives up after 1000 instead of running for minutes
@@ -54,6 +61,8 @@ class EulerSolver:
                 self.op.add_mg_level(level)
         _lib.call("atm_solver_init", self.op.handle, self.dt, case.Ma, case.Fr, float(eps),
                   int(max_its), int(precision))
+        if continue_on_not_converged:
+            _lib.call("atm_solver_set_continue_on_not_converged", self.op.handle, 1)
         self.n_scalar = self.op.n_scalar
         self.set_state(case.rho, case.u, case.p)
         alpha = np.ascontiguousarray(case.sponge_alpha, dtype=np.float64)
@@ -86,9 +95,22 @@ class EulerSolver:
         return dict(zip(keys, s.tolist()))
 
     def diagnostics(self):
+        """The printouts of Atmospheric_Flow.cc:1121-1122,1225-1235 for the
+        current state: min/max density, max celerity sqrt(gamma p/rho), max
+        |u| (device reductions at the nodes), and the Courant numbers
+        CFL_c = dt max_c k sqrt(dim) / (Ma h_min), CFL_u = dt max_u k sqrt(dim) / h_min
+        with h_min the smallest cell diameter."""
+        from .hill import min_cell_diameter
+
         out = np.zeros(4)
         _lib.call("atm_solver_diagnostics", self.op.handle, _d(out))
-        return dict(zip(("min_rho", "max_rho", "max_celerity", "max_velocity"), out.tolist()))
+        d = dict(zip(("min_rho", "max_rho", "max_celerity", "max_velocity"), out.tolist()))
+        if not hasattr(self, "_hmin"):
+            self._hmin = min_cell_diameter(self.case.mapping_nodes, self.case.params.mapping_degree)
+        scale = self.dt * self.case.degree * np.sqrt(2.0) / self._hmin
+        d["cfl_c"] = scale * d["max_celerity"] / self.case.Ma
+        d["cfl_u"] = scale * d["max_velocity"]
+        return d
 
     # ------------------------------------------------- checkpoint / restart --
     def save(self, path):

@@ -48,6 +48,9 @@ class MemberRequest:
     steps: int
     precision: int = 1
     eps: float = 1e-8
+    # (rho, u, p) host arrays to start from instead of the case's initial
+    # data, e.g. a member resumed from a checkpoint (EulerSolver.save)
+    initial_state: tuple | None = None
 
 
 @dataclasses.dataclass
@@ -140,6 +143,8 @@ class Server:
             solver = EulerSolver(case, eps=req.eps, precision=req.precision,
                                  true_residual_check=req.precision != 0,
                                  stream=stream.value)
+            if req.initial_state is not None:
+                solver.set_state(*req.initial_state)
             left = req.steps
             while left > 0:
                 n = min(self.chunk, left)
@@ -185,6 +190,10 @@ class Server:
                                  true_residual_check=prec != 0, stream=stream.value,
                                  levels=b.levels if prec != 0 else None,
                                  sponge_target=b.u_target)
+            if any(r.initial_state is not None for r in reqs):
+                parts = [r.initial_state if r.initial_state is not None else (c.rho, c.u, c.p)
+                         for r, c in zip(reqs, cases)]
+                solver.set_state(*(np.concatenate([q[f] for q in parts]) for f in range(3)))
             target = [r.steps for r in reqs]
             steps = 0
             while steps < max(target):

@@ -279,7 +279,17 @@ int atm_solver_set_sponge_target(atm_handle h, const double *u_target);
  * reference counterpart (the reference writes VTU output only,
  * Atmospheric_Flow.cc:885-918). */
 int atm_solver_set_clock(atm_handle h, double time, long steps);
+/* Advance n_steps IMEX steps.  A Schur solve that reaches max_its ends the
+ * call with ATM_NOT_CONVERGED, as the reference's SolverControl throws and
+ * main returns 1 (Atmospheric_Flow.cc:1289-1311); a non-finite residual or
+ * Picard update ends it with ATM_NONFINITE.  The failed step is abandoned:
+ * the state, time and step count stay those of the last completed step (the
+ * state is written only in the final stage, which has no Krylov solve). */
 int atm_solver_run(atm_handle h, int n_steps);
+/* on = 1: a Schur solve that reaches max_its is counted (stats[5]) and the
+ * step carries on with the unconverged iterate; on = 0 (default): it fails
+ * as atm_solver_run says.  No reference counterpart (deal.II always throws). */
+int atm_solver_set_continue_on_not_converged(atm_handle h, int on);
 /* stats[0..8] as doubles: steps, Picard iterations (total), Krylov
  * iterations (total), last Picard count stage 1, stage 2, Krylov solves that
  * hit max_its, simulated time, current dt, V-cycles (total). */

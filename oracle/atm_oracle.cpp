@@ -10,7 +10,7 @@
 // machine, so its own FP64 MatrixFree run cannot be executed here and the
 // reference ships no golden vectors.  This restatement is checked against
 // analytic properties instead (exact quadrature, conservation, adjointness,
-// steady states) in tests/test_oracle_*.py.
+// steady states) in tests/test_oracle.py and tests/test_known_answer.py.
 //
 // What it restates (file:line refer to the reference project):
 //   * EULEROperator<dim=2,...>  euler_operator.h:24-2627
@@ -48,6 +48,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -1374,6 +1375,31 @@ void orc_solver_set_sponge(void *h, const double *alpha, double ubg0, double ubg
 void orc_solver_run(void *h, int n_steps) {
   Solver *s = static_cast<Solver *>(h);
   for (int i = 0; i < n_steps; ++i) s->step();
+}
+// Diagnostics of the state after a completed step, Atmospheric_Flow.cc:991-1087:
+// get_min_density / get_max_density (rho_curr == rho_old after the step,
+// :1221), compute_max_celerity (sqrt(Cp_Cv p / rho), pres_old and rho_old) and
+// get_max_velocity (|u_old|).  The reference evaluates FE_DGQ fields with
+// QGaussLobatto(k+1), whose points are the element's own support points, so the
+// values are the nodal coefficients.  Its celerity maximum starts from
+// numeric_limits<double>::min() and its velocity maximum from 0.
+// out[0..3] = min rho, max |rho|, max celerity, max |u|.
+void orc_solver_diagnostics(void *h, double *out) {
+  Solver *s = static_cast<Solver *>(h);
+  const long ns = s->op.ns();
+  const int nn2 = s->op.nn2;
+  double rmin = std::numeric_limits<double>::max(), rmax = 0.0;
+  double cmax = std::numeric_limits<double>::min(), umax = 0.0;
+  for (long i = 0; i < ns; ++i) {
+    const long c = i / nn2, j = i % nn2;
+    const double r = s->rho_old[i];
+    rmin = std::min(rmin, r);
+    rmax = std::max(rmax, std::fabs(r));
+    cmax = std::max(cmax, std::sqrt(GAMMA_GAS * s->pres_old[i] / r));
+    const double ux = s->u_old[(2 * c) * nn2 + j], uz = s->u_old[(2 * c + 1) * nn2 + j];
+    umax = std::max(umax, std::sqrt(ux * ux + uz * uz));
+  }
+  out[0] = rmin; out[1] = rmax; out[2] = cmax; out[3] = umax;
 }
 // stats: picard_total, gmres_total, cg_total, solve_fail, inner_cg, picard1, picard2
 void orc_solver_stats(void *h, long *out) {

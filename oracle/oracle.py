@@ -3,7 +3,8 @@
 TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()``
 and the CPU-baseline / reference legs of ``bench.py`` -- never by the product
 package.  Parity against deal.II is unpinned (deal.II is not installed); the
-oracle is pinned by analytic properties in ``tests/test_oracle_*.py``.
+oracle is pinned by analytic properties in ``tests/test_oracle.py`` and
+``tests/test_known_answer.py``.
 """
 from __future__ import annotations
 
@@ -70,6 +71,7 @@ def lib():
                                             ctypes.c_double]
         L.orc_solver_run.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_solver_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_long)]
+        L.orc_solver_diagnostics.argtypes = [ctypes.c_void_p, _dp]
         L.orc_num_threads.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -236,6 +238,12 @@ class OracleSolver:
 
     def run(self, n_steps):
         lib().orc_solver_run(self.h, n_steps)
+
+    def diagnostics(self):
+        """min/max density, max celerity, max |u| (Atmospheric_Flow.cc:991-1087)."""
+        out = np.zeros(4)
+        lib().orc_solver_diagnostics(self.h, _d(out))
+        return dict(zip(("min_rho", "max_rho", "max_celerity", "max_velocity"), out.tolist()))
 
     def stats(self):
         out = (ctypes.c_long * 7)()

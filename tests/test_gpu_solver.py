@@ -43,6 +43,29 @@ def test_steps_match_oracle(cuda_ok, params, steps):
     assert sg["picard_total"] == so["picard_total"]
 
 
+def test_diagnostics_match_oracle(cuda_ok):
+    """min/max rho, max celerity and max |u| (Atmospheric_Flow.cc:991-1087)
+    after 3 steps agree with the oracle's to 1e-10 relative, and the Courant
+    numbers follow the reference's formula (:1227-1234)."""
+    from atmospheric_flows_gb300.euler_solver import EulerSolver
+    from atmospheric_flows_gb300.hill import min_cell_diameter
+
+    case = build_case(HillParams(nx=10, nz=5, degree=3, cfl=3.0, theta_noise=0.1, seed=4))
+    g = EulerSolver(case, eps=EPS)
+    o = OracleSolver(case, eps=EPS, inner_tol=1e-15)
+    g.run(3)
+    o.run(3)
+    dg, do = g.diagnostics(), o.diagnostics()
+    for key in ("min_rho", "max_rho", "max_celerity", "max_velocity"):
+        assert abs(dg[key] - do[key]) <= 1e-10 * abs(do[key]), (key, dg[key], do[key])
+    h = min_cell_diameter(case.mapping_nodes, case.params.mapping_degree)
+    cfl_c = case.dt * do["max_celerity"] / case.Ma * case.degree * np.sqrt(2.0) / h
+    assert abs(dg["cfl_c"] - cfl_c) <= 1e-10 * cfl_c
+    # the case's dt was chosen for acoustic CFL 3 on the initial state
+    assert 2.5 < dg["cfl_c"] < 3.5
+    g.close()
+
+
 def test_bitwise_reproducible(cuda_ok):
     from atmospheric_flows_gb300.euler_solver import EulerSolver
 

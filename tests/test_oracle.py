@@ -216,3 +216,19 @@ def test_golden_fixture_regression_adaptive():
     for name, v in zip(("rho", "u", "p"), s.get_state()):
         ref = g[name]
         assert np.linalg.norm(v - ref) / np.linalg.norm(ref) < 1e-11, name
+
+
+def test_diagnostics_are_the_nodal_extrema(hill_case):
+    """The oracle's diagnostics (Atmospheric_Flow.cc:991-1087) are the
+    extrema over the nodal values of the state: FE_DGQ fields evaluated at
+    QGaussLobatto(k+1) points are their support-point coefficients."""
+    s = OracleSolver(hill_case, eps=1e-10)
+    rho, u, p = perturbed(hill_case, seed=8)
+    s.set_state(rho, u, p)
+    d = s.diagnostics()
+    nn2 = (hill_case.degree + 1) ** 2
+    uu = u.reshape(-1, 2, nn2)
+    assert d["min_rho"] == np.min(rho)
+    assert d["max_rho"] == np.max(np.abs(rho))
+    assert abs(d["max_celerity"] - np.max(np.sqrt(1.4 * p / rho))) <= 1e-15 * d["max_celerity"]
+    assert abs(d["max_velocity"] - np.max(np.hypot(uu[:, 0], uu[:, 1]))) <= 1e-14 * d["max_velocity"]
