@@ -390,6 +390,61 @@ class AdaptParams:
     every: int = 50                 # steps between re-adaptations
 
 
+def coarser_tree(tree: QuadTree) -> QuadTree | None:
+    """The tree with its finest cells merged into their parents, or None when
+    nothing is refined.  All children of a deepest refined node are leaves,
+    and merging every deepest group keeps the 2:1 balance."""
+    if not tree.refined:
+        return None
+    top = max(n[0] for n in tree.refined)
+    out = QuadTree(tree.nx, tree.nz, tree.periodic, tree.max_level)
+    out.refined = {n for n in tree.refined if n[0] < top}
+    return out
+
+
+def mg_hierarchy_adaptive(p: HillParams, tree: QuadTree, max_levels: int = 8) -> list:
+    """Coarse levels of the multigrid Schur preconditioner on an adaptive mesh
+    (fine to coarse, the leaf mesh itself excluded).
+
+    Each level merges the finest 2x2 groups of the level above and keeps
+    every other cell, so levels may have hanging faces; once the base mesh is
+    reached the uniform 2x2 coarsening of ``hill.mg_hierarchy`` continues.
+    ``children[n_cells][4]`` lists the merged cells at positions (x-,z-),
+    (x+,z-), (x-,z+), (x+,z+), or (cell, -1, -1, -1) for a cell that stays.
+    A merged cell's mapping is its base cell's mapping on the union of the
+    four sub-squares, so the children are exact sub-squares of the parent
+    and the prolongation is the exact polynomial embedding."""
+    from .hill import mg_hierarchy
+
+    base_nodes = build_mesh(p)[0]
+    levels = []
+    cur = tree
+    while len(levels) + 1 < max_levels:
+        nxt = coarser_tree(cur)
+        if nxt is None:
+            break
+        cidx = cur.leaf_index()
+        ch = []
+        for node in nxt.leaves():
+            if node in cidx:
+                ch.append((cidx[node], -1, -1, -1))
+            else:
+                l, ix, iz = node
+                ch.append(tuple(cidx[(l + 1, 2 * ix + a, 2 * iz + b)]
+                                for b in range(2) for a in range(2)))
+        inner, bdry = nxt.face_tables()
+        levels.append(dict(n_cells=len(ch),
+                           mapping_nodes=np.ascontiguousarray(
+                               leaf_mapping_nodes(nxt, base_nodes, p.mapping_degree)),
+                           inner_faces=inner, boundary_faces=bdry,
+                           children=np.asarray(ch, dtype=np.int32).reshape(-1, 4)))
+        cur = nxt
+    if not cur.refined and len(levels) + 1 < max_levels:
+        # the uniform base mesh numbers its cells as the unrefined tree does
+        levels.extend(mg_hierarchy(p, max_levels=max_levels - len(levels)))
+    return levels
+
+
 def adaptive_case(p: HillParams, tree: QuadTree, state=None, dt=None) -> HillCase:
     """HillCase on the leaves of `tree`; `state` = (rho, u, p) on those leaves
     or None for the initial condition interpolated from the base mesh."""
@@ -422,7 +477,8 @@ def adaptive_case(p: HillParams, tree: QuadTree, state=None, dt=None) -> HillCas
     return HillCase(params=p, n_cells=nc, mapping_nodes=np.ascontiguousarray(nodes),
                     inner_faces=inner, boundary_faces=bdry, node_xz=xz,
                     rho=np.ascontiguousarray(rho), u=np.ascontiguousarray(u),
-                    p=np.ascontiguousarray(pres), sponge_alpha=alpha.reshape(-1), dt=dt)
+                    p=np.ascontiguousarray(pres), sponge_alpha=alpha.reshape(-1), dt=dt,
+                    tree=tree)
 
 
 def mark(tree: QuadTree, indicator: np.ndarray, ap: AdaptParams):
@@ -475,10 +531,14 @@ class AdaptiveMember:
         self.time = 0.0
 
     def _make_solver(self):
-        if self.precision != 0:
-            raise ValueError("adaptive meshes run the reference Schur solver (precision 0); "
-                             "the multigrid hierarchy needs a conforming mesh")
-        return self._Solver(self.case, eps=self.eps, precision=0, dt=self.dt, stream=self.stream)
+        if self.precision == 0:
+            return self._Solver(self.case, eps=self.eps, precision=0, dt=self.dt,
+                                stream=self.stream)
+        # multigrid Schur solve: the hierarchy of this leaf mesh, rebuilt
+        # after every adaptation; stop on the true residual (S is nonlinear)
+        return self._Solver(self.case, eps=self.eps, precision=self.precision, dt=self.dt,
+                            stream=self.stream, true_residual_check=True,
+                            levels=mg_hierarchy_adaptive(self.p, self.tree))
 
     def _adapt_state(self, rho, u, pres):
         k, m = self.p.degree, self.p.mapping_degree

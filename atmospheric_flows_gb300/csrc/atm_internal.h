@@ -111,6 +111,9 @@ struct atm_ctx {
   bool autotune = true;  // choose the face kernels' cells per block by timing
   mutable atm::KTimer timer;
   bool capturing = false;  // a CUDA graph is being recorded: timers are off
+  // device address of the static Schur scratch array in this handle's
+  // context (atm_schur_vmult_static_scratch; looked up on first use)
+  void *static_scratch = nullptr;
   long n_scalar() const { return (long)nc * nn2; }
   long n_vector() const { return 2L * nc * nn2; }
 };

@@ -17,10 +17,16 @@ namespace atm {
 
 int upload_basis_impl(const double *t) { return upload_basis_here(t); }
 
-// hanging-face instantiations of B and C/D live in hang_schur.cu
+// hanging-face instantiations of B and C/D live in hang_schur.cu (FP64) and
+// hang_schur_f.cu (FP32 multigrid levels)
 int launch_B_hang(const atm_ctx &c, double *dst, const double *p, double coeff, int mode);
 int launch_CD_hang(const atm_ctx &c, double *dst, const double *w, const double *p,
                    double coeff, int mode);
+template <typename T>
+int level_B_hang(const OpView<T> &o, T *dst, const T *p, T cB, int mode);
+template <typename T>
+int level_CD_hang(const OpView<T> &o, T *dst, const T *w, const T *p, T cC, int mode,
+                  const ChebArgs<T> *ch);
 
 // ============================================================ mass apply ===
 // dst = M_w src for NCOMP components; weight tile (rho) or constant scale
@@ -396,16 +402,19 @@ int launch_block_apply(const atm_ctx &c, double *dst, const double *src, const d
 template <typename T>
 int level_B(const LevelViewT<T> &v, T *dst, const T *p, T cB, int mode) {
   OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune, v.pfix, v.pfq, v.pff};
+  if (v.mesh.nhang > 0) return level_B_hang<T>(o, dst, p, cB, mode);
   ATM_DISPATCH_K(v.k, (B_launch<K, T, false>(o, dst, p, cB, mode)));
 }
 template <typename T>
 int level_CD(const LevelViewT<T> &v, T *dst, const T *w, const T *p, T cC, int mode) {
   OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune, v.pfix, v.pfq, v.pff};
+  if (v.mesh.nhang > 0) return level_CD_hang<T>(o, dst, w, p, cC, mode, nullptr);
   ATM_DISPATCH_K(v.k, (CD_launch<K, T, false>(o, dst, w, p, cC, mode)));
 }
 template <typename T>
 int level_CD_cheb(const LevelViewT<T> &v, const T *w, T cC, const ChebArgs<T> &ch) {
   OpView<T> o{v.k, v.nc, v.mesh, v.ainv, v.invd, v.st, v.tune, v.pfix, v.pfq, v.pff};
+  if (v.mesh.nhang > 0) return level_CD_hang<T>(o, nullptr, w, ch.x, cC, 4, &ch);
   ATM_DISPATCH_K(v.k, (CD_launch<K, T, false>(o, nullptr, w, ch.x, cC, 4, &ch)));
 }
 template <typename T>

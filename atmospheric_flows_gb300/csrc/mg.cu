@@ -7,12 +7,15 @@
 // hierarchies only for its mass-type systems (Atmospheric_Flow.cc:456-522:
 // smoothing range 15, degree 3, 10 eigenvalue iterations).  Here the same
 // smoother recipe is applied to the Schur/Helmholtz operator itself:
-//   * level 0 is the operator mesh; level l+1 is made of 2x2 cells of level l
+//   * level 0 is the operator mesh; level l+1 merges groups of 2x2 cells of
+//     level l (on a 2:1 adaptive mesh, the finest cells first; the other
+//     cells stay as they are, so coarse levels may have hanging faces too)
 //     and carries a rediscretisation of S = D - C A^{-1} B on that mesh (the
 //     FP64 operator kernels instantiated for the level's scalar type), with
 //     rho_fix and p_fix injected level by level and A^{-1} rebuilt per level;
 //   * transfer is the exact embedding of the coarse polynomial space into the
-//     four children (prolongation) and its transpose (restriction);
+//     four children (prolongation) and its transpose (restriction); a cell
+//     that is not merged is copied;
 //   * smoother: Chebyshev of degree 3 preconditioned by the inverse diagonal
 //     of D on [1.2 lambda_max / 15, 1.2 lambda_max], lambda_max from 10 power
 //     iterations; the coarsest level runs a higher-degree Chebyshev.
@@ -38,7 +41,7 @@ struct MGLevelT {
   int nc = 0;
   MeshT<T> mesh;
   int *parent = nullptr;    // [nc] cell of level+1 containing this cell
-  int *ppos = nullptr;      // [nc] position a + 2b of this cell inside its parent
+  int *ppos = nullptr;      // [nc] position a + 2b of this cell inside its parent (4: same cell)
   int *children = nullptr;  // [nc][4] cells of level-1 (levels >= 1)
   T *ainv = nullptr, *invd = nullptr, *rho = nullptr, *pfix = nullptr;
   T *pfq = nullptr, *pff = nullptr;  // p_fix at quadrature points / face traces
@@ -175,6 +178,10 @@ __global__ void k_prolong_add(T *__restrict__ fine, const T *__restrict__ coarse
   const int iz = i / NN, ix = i - iz * NN;
   const int pos = ppos[cf], a = pos & 1, b = pos >> 1;
   const T *u = coarse + (long)parent[cf] * NN2;
+  if (pos == 4) {  // cell unchanged on the coarser level
+    fine[g] += u[i];
+    return;
+  }
   T s = 0;
 #pragma unroll
   for (int jz = 0; jz < NN; ++jz) {
@@ -194,6 +201,10 @@ __global__ void k_restrict(T *__restrict__ coarse, const T *__restrict__ fine,
   if (g >= (long)ncc * NN2) return;
   const int cc = (int)(g / NN2), j = (int)(g - (long)cc * NN2);
   const int jz = j / NN, jx = j - jz * NN;
+  if (children[cc * 4 + 1] < 0) {  // cell unchanged on this level
+    coarse[g] = fine[(long)children[cc * 4] * NN2 + j];
+    return;
+  }
   T s = 0;
 #pragma unroll
   for (int pos = 0; pos < 4; ++pos) {
@@ -218,6 +229,10 @@ __global__ void k_inject(T *__restrict__ coarse, const T *__restrict__ fine,
   if (g >= (long)ncc * NN2) return;
   const int cc = (int)(g / NN2), j = (int)(g - (long)cc * NN2);
   const int jz = j / NN, jx = j - jz * NN;
+  if (children[cc * 4 + 1] < 0) {  // cell unchanged on this level
+    coarse[g] = fine[(long)children[cc * 4] * NN2 + j];
+    return;
+  }
   const int child = children[cc * 4 + tb.fa[jx] + 2 * tb.fa[jz]];
   const T *u = fine + (long)child * NN2;
   T s = 0;
@@ -267,6 +282,7 @@ MGHier<double> &hier<double>(MG &mg) { return mg.d; }
 template <typename T>
 void level_free(MGLevelT<T> &L) {
   cudaFree(L.mesh.qgeo); cudaFree(L.mesh.fgeo); cudaFree(L.mesh.nbr); cudaFree(L.mesh.nbrf);
+  cudaFree(L.mesh.hnb); cudaFree(L.mesh.hgeo);
   cudaFree(L.parent); cudaFree(L.ppos); cudaFree(L.children);
   cudaFree(L.ainv); cudaFree(L.invd); cudaFree(L.rho); cudaFree(L.pfix);
   cudaFree(L.pfq); cudaFree(L.pff);
@@ -326,6 +342,16 @@ int level_alloc(atm_ctx &c, MGLevelT<T> &L, const HostMesh &hm) {
   ATM_CUDA(cudaMemcpyAsync(L.mesh.fgeo, ff.data(), ff.size() * sizeof(T), cudaMemcpyHostToDevice, c.stream));
   ATM_CUDA(cudaMemcpyAsync(L.mesh.nbr, hm.nbr.data(), hm.nbr.size() * sizeof(int), cudaMemcpyHostToDevice, c.stream));
   ATM_CUDA(cudaMemcpyAsync(L.mesh.nbrf, hm.nbrf.data(), hm.nbrf.size() * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+  L.mesh.nhang = hm.nhang;
+  if (hm.nhang > 0) {
+    std::vector<T> hg(hm.hgeo.begin(), hm.hgeo.end());
+    ATM_CUDA(cudaMalloc(&L.mesh.hnb, hm.hnb.size() * sizeof(int)));
+    ATM_CUDA(cudaMalloc(&L.mesh.hgeo, hg.size() * sizeof(T)));
+    ATM_CUDA(cudaMemcpyAsync(L.mesh.hnb, hm.hnb.data(), hm.hnb.size() * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    ATM_CUDA(cudaMemcpyAsync(L.mesh.hgeo, hg.data(), hg.size() * sizeof(T), cudaMemcpyHostToDevice, c.stream));
+    // the host copies above are pageable: finish them before `hg` goes away
+    ATM_CUDA(cudaStreamSynchronize(c.stream));
+  }
   T **vecs[] = {&L.invd, &L.rho, &L.pfix, &L.x, &L.b, &L.r, &L.t, &L.d};
   for (T **v : vecs) {
     ATM_CUDA(cudaMalloc(v, ns * sizeof(T)));
@@ -353,11 +379,17 @@ int build_hier(atm_ctx &c, MG &mg) {
       const std::vector<int> &ch = mg.children[l];
       MGLevelT<T> &F = H.lv[l - 1];
       std::vector<int> parent(F.nc, -1), ppos(F.nc, -1);
-      for (int cc = 0; cc < H.lv[l].nc; ++cc)
+      for (int cc = 0; cc < H.lv[l].nc; ++cc) {
+        if (ch[4 * cc + 1] < 0) {  // the cell is unchanged on this level
+          parent[ch[4 * cc]] = cc;
+          ppos[ch[4 * cc]] = 4;
+          continue;
+        }
         for (int p = 0; p < 4; ++p) {
           parent[ch[4 * cc + p]] = cc;
           ppos[ch[4 * cc + p]] = p;
         }
+      }
       ATM_CUDA(cudaMalloc(&F.parent, F.nc * sizeof(int)));
       ATM_CUDA(cudaMalloc(&F.ppos, F.nc * sizeof(int)));
       ATM_CUDA(cudaMalloc(&H.lv[l].children, ch.size() * sizeof(int)));
@@ -648,11 +680,6 @@ int mg_add_level(atm_ctx &c, int n_cells, int mapdeg, const double *nodes, int n
     set_error("atm_mg_add_level: need n_cells >= 1 and a children table");
     return ATM_BAD_ARG;
   }
-  if (c.mesh.nhang > 0) {
-    set_error("atm_mg_add_level: the multigrid hierarchy needs a conforming mesh "
-              "(this mesh has hanging faces)");
-    return ATM_BAD_ARG;
-  }
   if (!c.mg) {
     MG *mg = new MG();
     HostMesh hm;
@@ -660,10 +687,17 @@ int mg_add_level(atm_ctx &c, int n_cells, int mapdeg, const double *nodes, int n
     hm.fgeo.resize((size_t)c.nc * 4 * 3 * c.nq);
     hm.nbr.resize((size_t)c.nc * 4);
     hm.nbrf.resize((size_t)c.nc * 4);
+    hm.nhang = c.mesh.nhang;
+    hm.hnb.resize((size_t)c.mesh.nhang * 2);
+    hm.hgeo.resize((size_t)c.mesh.nhang * 2 * 3 * c.nq);
     ATM_CUDA(cudaMemcpyAsync(hm.qgeo.data(), c.mesh.qgeo, hm.qgeo.size() * 8, cudaMemcpyDeviceToHost, c.stream));
     ATM_CUDA(cudaMemcpyAsync(hm.fgeo.data(), c.mesh.fgeo, hm.fgeo.size() * 8, cudaMemcpyDeviceToHost, c.stream));
     ATM_CUDA(cudaMemcpyAsync(hm.nbr.data(), c.mesh.nbr, hm.nbr.size() * 4, cudaMemcpyDeviceToHost, c.stream));
     ATM_CUDA(cudaMemcpyAsync(hm.nbrf.data(), c.mesh.nbrf, hm.nbrf.size() * 4, cudaMemcpyDeviceToHost, c.stream));
+    if (hm.nhang > 0) {
+      ATM_CUDA(cudaMemcpyAsync(hm.hnb.data(), c.mesh.hnb, hm.hnb.size() * 4, cudaMemcpyDeviceToHost, c.stream));
+      ATM_CUDA(cudaMemcpyAsync(hm.hgeo.data(), c.mesh.hgeo, hm.hgeo.size() * 8, cudaMemcpyDeviceToHost, c.stream));
+    }
     ATM_CUDA(cudaStreamSynchronize(c.stream));
     mg->hm.push_back(std::move(hm));
     mg->ncells.push_back(c.nc);
@@ -678,27 +712,33 @@ int mg_add_level(atm_ctx &c, int n_cells, int mapdeg, const double *nodes, int n
   }
   MG &mg = *c.mg;
   const int nfine = mg.ncells.back();
-  if (4L * n_cells != nfine) {
-    set_error("atm_mg_add_level: a coarse level must have a quarter of the cells of the "
-              "level above it");
-    return ATM_BAD_ARG;
-  }
+  // a row is four cells of the finer level (a merged cell) or one cell and
+  // three -1 (a cell that stays as it is: adaptive meshes coarsen their
+  // finest cells first); every finer cell appears exactly once
   std::vector<int> seen(nfine, 0), ch(children, children + 4L * n_cells);
-  for (size_t i = 0; i < ch.size(); ++i) {
-    if (ch[i] < 0 || ch[i] >= nfine || seen[ch[i]]) {
-      set_error("atm_mg_add_level: children table entry " + std::to_string(i) +
-                " out of range or repeated");
-      return ATM_BAD_ARG;
+  long covered = 0;
+  for (int cc = 0; cc < n_cells; ++cc) {
+    const int *r = &ch[4L * cc];
+    const bool same = r[1] < 0 && r[2] < 0 && r[3] < 0;
+    for (int q = 0; q < (same ? 1 : 4); ++q) {
+      if (r[q] < 0 || r[q] >= nfine || seen[r[q]]) {
+        set_error("atm_mg_add_level: children row " + std::to_string(cc) +
+                  " has an entry out of range or repeated (rows are 4 finer cells, or one "
+                  "finer cell and three -1)");
+        return ATM_BAD_ARG;
+      }
+      seen[r[q]] = 1;
+      ++covered;
     }
-    seen[ch[i]] = 1;
+  }
+  if (covered != nfine || n_cells >= nfine) {
+    set_error("atm_mg_add_level: the children table must cover every cell of the finer level "
+              "exactly once and merge at least one group");
+    return ATM_BAD_ARG;
   }
   HostMesh hm;
   int rc = build_mesh_tables(c.k, n_cells, mapdeg, nodes, n_inner, inner, n_bdry, bdry, hm);
   if (rc) return rc;
-  if (hm.nhang > 0) {
-    set_error("atm_mg_add_level: coarse levels must be conforming meshes");
-    return ATM_BAD_ARG;
-  }
   mg.hm.push_back(std::move(hm));
   mg.ncells.push_back(n_cells);
   mg.children.push_back(std::move(ch));

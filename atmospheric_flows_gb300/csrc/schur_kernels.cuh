@@ -341,10 +341,8 @@ int CD_launch(const OpView<T> &v, T *dst, const T *w, const T *p, T cC, int mode
         mode == 0 ? k_CD<K, 0, T, HG>
         : mode == 1 ? k_CD<K, 1, T, HG>
         : mode == 2 ? k_CD<K, 2, T, HG>
-                    : k_CD<K, 3, T, HG>;
-    if constexpr (!HG) {  // the fused smoother step runs on conforming levels only
-      if (mode == 4) fn = k_CD<K, 4, T, HG>;
-    }
+        : mode == 3 ? k_CD<K, 3, T, HG>
+                    : k_CD<K, 4, T, HG>;
     if (sm > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
       if (e != cudaSuccess) return e;

@@ -20,13 +20,15 @@
 //     overwrites every entry it later reads.  Calls whose kernels overlap on
 //     the GPU (other streams, other threads, other contexts) race on it; the
 //     caller must serialise them.
-//   * the device address of the array is looked up once per device, by the
-//     first call made while that device is current; make that first call
-//     before any stream capture.
+//   * the device address of the array is looked up by the first call made
+//     with a handle, in the CUDA context that handle's memory belongs to
+//     (its device, current at the call), and kept in the handle.  A handle
+//     is bound to one context, so the address stays valid for the handle's
+//     life; after a device reset every old handle is dead and new handles
+//     look the address up again.  Make that first call before any stream
+//     capture.
 //   * kernel timing (atm_timing_enable) must be off, because the timers
 //     create CUDA events on demand.
-#include <mutex>
-
 #include "atm_device.cuh"
 
 namespace atm {
@@ -35,20 +37,15 @@ constexpr long SCHUR_SCRATCH_DOUBLES = 1L << 20;  // 8 MiB
 static __device__ __align__(256) double g_schur_scratch[SCHUR_SCRATCH_DOUBLES];
 
 namespace {
-constexpr int MAX_DEVICES = 64;
-std::mutex g_mu;
-double *g_addr[MAX_DEVICES] = {nullptr};
-
-// host-side stand-in -> device address, once per device (current device)
-int scratch_address(int dev, double **out) {
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
+// host-side stand-in -> device address in the current context, once per handle
+int scratch_address(atm_ctx &h, double **out) {
+  if (!h.static_scratch) {
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_schur_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_schur_scratch)");
-    g_addr[dev] = static_cast<double *>(p);
+    h.static_scratch = p;
   }
-  *out = g_addr[dev];
+  *out = static_cast<double *>(h.static_scratch);
   return ATM_OK;
 }
 }  // namespace
@@ -72,12 +69,12 @@ extern "C" int atm_schur_vmult_static_scratch(atm_handle h, double *dst, const d
   }
   int dev = -1;
   ATM_CUDA(cudaGetDevice(&dev));
-  if (dev != h->device || dev < 0 || dev >= MAX_DEVICES) {
+  if (dev != h->device) {
     set_error("atm_schur_vmult_static_scratch: make the context's device current");
     return ATM_BAD_ARG;
   }
   double *scratch = nullptr;
-  int rc = scratch_address(dev, &scratch);
+  int rc = scratch_address(*h, &scratch);
   if (rc) return rc;
   const double co = implicit_coeff(*h);
   // no tile-shape timing here (it would create events): tuned choices made by

@@ -22,6 +22,7 @@ int upload_basis_hang_rho(const double *t);
 int upload_basis_hang_vel(const double *t);
 int upload_basis_hang_pres(const double *t);
 int upload_basis_hang_schur(const double *t);
+int upload_basis_hang_schur_f(const double *t);
 
 // Legendre P_n(x) and P_n'(x) by the three-term recurrence
 static void legendre_pd(int n, double x, double *p, double *dp) {
@@ -142,7 +143,8 @@ int upload_basis_all() {
   }
   if (upload_basis_rhs(tab.data()) || upload_basis_impl(tab.data()) ||
       upload_basis_hang_rho(tab.data()) || upload_basis_hang_vel(tab.data()) ||
-      upload_basis_hang_pres(tab.data()) || upload_basis_hang_schur(tab.data())) {
+      upload_basis_hang_pres(tab.data()) || upload_basis_hang_schur(tab.data()) ||
+      upload_basis_hang_schur_f(tab.data())) {
     set_error("failed to upload basis tables to constant memory");
     return ATM_CUDA_ERROR;
   }

@@ -54,10 +54,16 @@ class EulerSolver:
         self.precision = int(precision)
         self.op.set_true_residual_check(true_residual_check)
         if self.precision in (self.PRECISION_MIXED, self.PRECISION_FP64_MG):
-            from .hill import mg_hierarchy
+            if levels is None:
+                if getattr(case, "tree", None) is not None:  # adaptive leaf mesh
+                    from .amr import mg_hierarchy_adaptive
 
-            for level in (levels if levels is not None
-                          else mg_hierarchy(case.params, max_levels=mg_levels)):
+                    levels = mg_hierarchy_adaptive(case.params, case.tree, max_levels=mg_levels)
+                else:
+                    from .hill import mg_hierarchy
+
+                    levels = mg_hierarchy(case.params, max_levels=mg_levels)
+            for level in levels:
                 self.op.add_mg_level(level)
         _lib.call("atm_solver_init", self.op.handle, self.dt, case.Ma, case.Fr, float(eps),
                   int(max_its), int(precision))

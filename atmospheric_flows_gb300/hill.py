@@ -101,6 +101,7 @@ class HillCase:
     dt: float
     Ma: float = MACH
     Fr: float = FROUDE
+    tree: object = None  # amr.QuadTree of an adaptive case (None: uniform mesh)
 
     @property
     def degree(self) -> int:

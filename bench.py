@@ -140,6 +140,16 @@ def workload(args):
             "parallelism": "one member per GPU (replicas)"}
 
 
+def gpu_uuid(device):
+    """nvidia-smi id ("GPU-<uuid>") of CUDA device `device` of this process."""
+    try:
+        import torch
+
+        return "GPU-" + str(torch.cuda.get_device_properties(device).uuid)
+    except Exception:
+        return str(device)
+
+
 class ClockSampler:
     """nvidia-smi clocks/throttle sampling during the timed region."""
 
@@ -147,8 +157,10 @@ class ClockSampler:
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index=0):
-        self.index = index
+    def __init__(self, device=0):
+        # nvidia-smi numbers GPUs physically and ignores CUDA_VISIBLE_DEVICES:
+        # name the CUDA device in use by its UUID
+        self.index = gpu_uuid(device)
         self.proc = None
         import tempfile
 
@@ -192,6 +204,10 @@ class ClockSampler:
             for name, v in zip(names, f[5:9]):
                 if v.lower().startswith("active"):
                     reasons.add(name)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
@@ -207,13 +223,13 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-# FP64 FMA throughput of this machine's GB300 (1255 GFLOP/s measured with an
-# independent-chain DFMA probe; profiles/fp64_fp32_fma_peak.md)
+# FP64 FMA throughput of the GB300 (1255 GFLOP/s, measured with the
+# independent-chain DFMA probe of `bench.py --fma-probe`)
 FP64_PEAK_TFLOPS = 1.255
 # DRAM bytes (read + write) per cell and launch of the dominant kernel families,
-# from `ncu` captures of this bench at 320x160 (profiles/k_CD_q4_320x160.md,
-# profiles/k_B_q4_320x160.md);
-# the traffic grows in proportion to the cell count.
+# from single-kernel `ncu` captures of this bench at 320x160 Q4: 311.0 MB per
+# k_CD<4,2> launch and 469.6 MB per k_B<4,2> launch over 51,200 cells; the
+# traffic grows in proportion to the cell count.
 NCU_TRAFFIC_PER_CELL = {4: {"CD": 311.0e6 / 51200, "B": 469.6e6 / 51200}}
 
 

@@ -174,8 +174,10 @@ int atm_diagonal_inverse(atm_handle h, double *dst);
  * synchronisation of cudaMalloc/cudaFree).  No counterpart in the reference.
  * Limits: 2*n_scalar <= 1048576 doubles, else ATM_BAD_ARG; all calls on a
  * device share the array, so calls that overlap on the GPU race; the first
- * call on a device looks the array up and should come before any stream
- * capture; kernel timing must be off.  Device pointers, context's stream. */
+ * call with a handle looks the array's address up in the handle's CUDA
+ * context (kept in the handle, so it stays right across contexts and device
+ * resets) and should come before any stream capture; kernel timing must be
+ * off.  Device pointers, context's stream. */
 int atm_schur_vmult_static_scratch(atm_handle h, double *dst, const double *src);
 
 /* Solve op x = b for the current NS stage.  Replaces the stage solvers'

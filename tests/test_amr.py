@@ -248,3 +248,67 @@ def test_oracle_hanging_identities_all_degrees(k):
     lhs = np.dot(of.vmult_pressure(q), w) * fc.Ma ** 2
     rhs = -np.dot(of.vmult_enthalpy(w), q) / (1.4 / 0.4 * 0.9)
     assert abs(lhs - rhs) / abs(lhs) < 1e-11
+
+
+@pytest.mark.parametrize("periodic", [True, False])
+def test_adaptive_multigrid_hierarchy(periodic):
+    """Levels of the multigrid Schur preconditioner on a 2:1 mesh: each level
+    merges the finest 2x2 groups of the level above (rows of 4 cells) and
+    keeps the rest (rows (cell, -1, -1, -1)), covers every finer cell once,
+    passes the library's own table checks (hanging faces included), puts a
+    merged cell's children exactly on its four sub-squares, and ends in the
+    uniform coarsening of the base mesh."""
+    import ctypes
+
+    from atmospheric_flows_gb300 import _lib
+    from atmospheric_flows_gb300.hill import gll_points, lagrange_matrix, mg_hierarchy
+
+    L = _lib.load()
+    p = HillParams(nx=8, nz=4, degree=2, periodic=periodic)
+    tree = amr.example_tree(p.nx, p.nz, p.periodic)
+    case = amr.adaptive_case(p, tree)
+    levels = amr.mg_hierarchy_adaptive(p, tree)
+    m = p.mapping_degree
+    n_fine, fine_nodes = case.n_cells, case.mapping_nodes
+    merged_levels = 0
+    n_adapt, t = 0, amr.coarser_tree(tree)
+    while t is not None:
+        n_adapt, t = n_adapt + 1, amr.coarser_tree(t)
+    assert n_adapt == tree.max_level
+    for il, lv in enumerate(levels):
+        ch = lv["children"]
+        assert ch.shape == (lv["n_cells"], 4)
+        same = np.all(ch[:, 1:] < 0, axis=1)
+        cells = np.concatenate([ch[same, 0], ch[~same].ravel()])
+        assert sorted(cells.tolist()) == list(range(n_fine))  # n_fine: the level above
+        assert np.any(~same)
+        merged_levels += int(np.any(same))
+        nh = ctypes.c_int(-1)
+        nodes = np.ascontiguousarray(lv["mapping_nodes"], dtype=np.float64)
+        rc = L.atm_check_mesh(p.degree, lv["n_cells"], m,
+                              nodes.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                              len(lv["inner_faces"]), lv["inner_faces"].ctypes.data,
+                              len(lv["boundary_faces"]), lv["boundary_faces"].ctypes.data,
+                              ctypes.byref(nh))
+        assert rc == 0, L.atm_last_error()
+        n_fine_prev, fine_prev = n_fine, fine_nodes
+        n_fine, fine_nodes = lv["n_cells"], nodes
+        if il >= n_adapt:
+            # uniform coarsening of the base mesh: each level is meshed on the
+            # terrain again (as the conforming hierarchy is)
+            continue
+        # unchanged cells keep their geometry; merged children are sub-squares
+        pn = nodes.reshape(-1, m + 1, m + 1, 2)
+        fine_nodes_l = fine_prev
+        fn = np.asarray(fine_nodes_l).reshape(-1, m + 1, m + 1, 2)
+        assert np.array_equal(pn[same], fn[ch[same, 0]])
+        ref = gll_points(m)
+        for a in range(2):
+            for b in range(2):
+                La = lagrange_matrix(ref, 0.5 * (a + ref))
+                Lb = lagrange_matrix(ref, 0.5 * (b + ref))
+                sub = np.einsum("zb,xa,cbad->czxd", Lb, La, pn[~same])
+                assert np.allclose(sub, fn[ch[~same, a + 2 * b]], rtol=0, atol=1e-8)
+    assert merged_levels == tree.max_level  # the adaptive part keeps cells on each level
+    uniform = mg_hierarchy(p)
+    assert [lv["n_cells"] for lv in levels[-len(uniform):]] == [u["n_cells"] for u in uniform]

@@ -20,7 +20,7 @@ NOT_CONVERGED, NONFINITE = 2, 3
 
 
 def _case():
-    return build_case(HillParams(nx=10, nz=5, degree=3, cfl=4.0))
+    return build_case(HillParams(nx=16, nz=8, degree=3, cfl=4.0))
 
 
 @pytest.mark.parametrize("precision", [0, 1])
