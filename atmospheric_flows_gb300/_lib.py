@@ -73,6 +73,8 @@ SIGNATURES = {
     "atm_solver_run": (_i, [_h, _i]),
     "atm_solver_set_continue_on_not_converged": (_i, [_h, _i]),
     "atm_solver_stats": (_i, [_h, _dp]),
+    "atm_set_members": (_i, [_h, _i, ctypes.POINTER(ctypes.c_int), _dp]),
+    "atm_member_stats": (_i, [_h, _i, _dp]),
     "atm_solver_diagnostics": (_i, [_h, _dp]),
 }
 

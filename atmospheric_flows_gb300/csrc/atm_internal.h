@@ -27,6 +27,7 @@ struct Tableau {
 // Per-stage weights handed to the explicit-operator kernels.
 struct Solver;
 struct MG;
+struct Members;
 
 struct StageCoef {
   double ca[3];  // explicit advection weights (a / b)
@@ -76,6 +77,11 @@ struct MeshT {
   int nhang = 0;
   int *hnb = nullptr;
   T *hgeo = nullptr;
+  // [nc] per-cell multiplier of the time step (null: 1).  A context that
+  // holds several members gives each member's cells dt_member / dt, so
+  // every dt-weighted term (stage fluxes, gravity, B, C, sponge) uses the
+  // member's own step; members share no faces, so a row scale is exact.
+  T *dts = nullptr;
 };
 using Mesh = MeshT<double>;
 
@@ -106,6 +112,7 @@ struct atm_ctx {
   double *dsmall = nullptr;  // device scratch for Hessenberg columns / y
   atm::Solver *solver = nullptr;
   atm::MG *mg = nullptr;  // multigrid hierarchy of the FGMRES Schur solves
+  atm::Members *mem = nullptr;  // several independent members in one context
   // GMRES/FGMRES only stop on a recomputed true residual (S is nonlinear)
   bool true_residual_check = false;
   bool autotune = true;  // choose the face kernels' cells per block by timing
@@ -216,7 +223,7 @@ int vec_maxdiff(cudaStream_t st, const double *a, const double *b, long n, doubl
 int vec_diagnostics(cudaStream_t st, const double *rho, const double *u, const double *p,
                     int nc, int nn2, double *red, double *out);
 int vec_sponge(cudaStream_t st, double *u, const double *alpha, double dt, double ub0,
-               double ub1, const double *target, int nc, int nn2);
+               double ub1, const double *target, const double *dts, int nc, int nn2);
 
 // ------------------------------------------------------------- MG levels --
 // Operator data of one multigrid level (T = float: mixed precision; double:
@@ -344,6 +351,59 @@ struct Solver {
   double *alpha;
   double *pool = nullptr;
 };
+
+// ------------------------------------------------- members of a batch --
+// A context may hold several independent members whose cells are
+// contiguous ranges and share no faces (a concatenated cell list).  Each
+// member then has its own time step (the per-cell dt multiplier), its own
+// Krylov solves (member-wise inner products, Hessenberg matrices and stops)
+// and its own Picard stop; a member whose solve fails is frozen and reported
+// without stopping the others.
+struct Members {
+  int n = 0;
+  std::vector<int> off;        // [n+1] first cell of each member
+  std::vector<double> dt;      // [n] each member's time step
+  std::vector<double> dts_host;  // [nc] dt multiplier of every cell
+  int *cell_mem = nullptr;     // [nc] member of each cell (device)
+  long *eoff = nullptr;        // [n+1] first scalar-vector element of each member
+  double *dts = nullptr;       // [nc] dt multiplier (device; mesh.dts points here)
+  double *red = nullptr;       // partial sums [rows][n][sb] (device)
+  double *out = nullptr;       // reduced values [rows][n] (device)
+  double *h_out = nullptr;     // pinned host mirror of out
+  double *coef = nullptr;      // coefficients [cols][n] (device)
+  double *h_coef = nullptr;    // pinned host staging of coef
+  int sb = 1;                  // reduction blocks per member
+  // per-member solver record
+  std::vector<int> status;     // ATM_OK, or the sticky failure of the member
+  std::vector<long> picard, krylov, fail_step;
+  std::vector<char> active;    // takes part in the current Picard loop / solve
+  std::vector<int> last_its;   // Krylov iterations of the last solve
+  std::vector<double> last_res;
+};
+constexpr int MEM_ROWS = 72;  // reduced rows per call (2 x 32 Hessenberg + 8)
+int members_set(atm_ctx &c, int n, const int *cell_off, const double *dt);
+void members_free(atm_ctx &c);
+int members_refresh_dt(atm_ctx &c);  // after a change of c.dt
+// member-wise reductions: out[col * n + m] (device, then copied to h_out)
+int seg_multidot(atm_ctx &c, const double *V, long ldv, int m, const double *w);
+int seg_maxdiff(atm_ctx &c, const double *a, const double *b);  // rows 0, 1
+int seg_read(atm_ctx &c, int rows);                             // out -> h_out (sync)
+// member-wise vector updates with coefficients coef[col * n + m] (host
+// values in h_coef, copied to the device first)
+int seg_multiaxpy(atm_ctx &c, double *w, const double *V, long ldv, int cols, double sign);
+int seg_scale(atm_ctx &c, double *d, const double *s);  // d = coef[member] * s
+// Schur solve of every active member: precision 0 GMRES + Jacobi (left),
+// 1/2 FGMRES + multigrid (FP32/FP64 V-cycle).  tol[m] as the solo solvers'.
+// Per-member iterations, residuals and outcomes in last_its / last_res and
+// `state` (ATM_OK, ATM_NOT_CONVERGED, ATM_NONFINITE; -1 for inactive members).
+int krylov_members(atm_ctx &c, int precision, double *x, const double *b,
+                   const std::vector<double> &tol, int maxit, std::vector<int> &state);
+// multigrid pieces used by krylov_members (mg.cu)
+int mg_prepare(atm_ctx &c, int precision);
+int mg_vcycle_only(atm_ctx &c, int precision, double *z, const double *v);
+double *mg_zbasis(atm_ctx &c);
+int mg_restart(const atm_ctx &c);
+void mg_invalidate(atm_ctx &c);  // device hierarchies are rebuilt on next use
 
 int solver_alloc(atm_ctx &c, Solver &s);
 void solver_free(Solver &s);

@@ -89,6 +89,7 @@ static void ctx_free(atm_ctx *c) {
   cudaFree(c->krylov);
   cudaFree(c->dsmall);
   if (c->h_red) cudaFreeHost(c->h_red);
+  members_free(*c);
   mg_free(*c);
   for (cudaEvent_t e : c->timer.ev) cudaEventDestroy(e);
   delete c;
@@ -246,7 +247,7 @@ int atm_set_dt(atm_handle h, double dt) {
   CHECK_H(h);
   if (!(dt > 0.0)) { set_error("dt must be positive"); return ATM_BAD_ARG; }
   h->dt = dt;
-  return ATM_OK;
+  return members_refresh_dt(*h);
 }
 int atm_set_mach(atm_handle h, double v) {
   CHECK_H(h);
@@ -455,7 +456,7 @@ int atm_solver_init(atm_handle h, double dt, double mach, double froude, double 
   s->max_its = max_its;
   s->precision = precision;
   h->dt = dt; h->Ma = mach; h->Fr = froude;
-  return ATM_OK;
+  return members_refresh_dt(*h);
 }
 
 #define CHECK_S(h)                                             \
@@ -549,6 +550,33 @@ int atm_solver_run(atm_handle h, int n_steps) {
   }
   ATM_CUDA(cudaStreamSynchronize(h->stream));
   ATM_CUDA(cudaGetLastError());
+  return ATM_OK;
+}
+int atm_set_members(atm_handle h, int n_members, const int *cell_offsets,
+                    const double *member_dt) {
+  CHECK_H(h);
+  if (n_members < 0 || n_members == 1) {
+    set_error("atm_set_members: n_members must be 0 (one member) or >= 2");
+    return ATM_BAD_ARG;
+  }
+  return members_set(*h, n_members, cell_offsets, member_dt);
+}
+int atm_member_stats(atm_handle h, int n, double *out) {
+  CHECK_H(h);
+  CHECK_PTR(out, "out");
+  if (!h->mem || n != h->mem->n) {
+    set_error("atm_member_stats: n must equal the number of members (atm_set_members)");
+    return ATM_BAD_ARG;
+  }
+  const Members &M = *h->mem;
+  for (int m = 0; m < n; ++m) {
+    double *o = out + 5 * m;
+    o[0] = M.status[m];
+    o[1] = (double)M.picard[m];
+    o[2] = (double)M.krylov[m];
+    o[3] = (double)M.fail_step[m];
+    o[4] = M.dt[m];
+  }
   return ATM_OK;
 }
 int atm_solver_stats(atm_handle h, double *st) {

@@ -180,13 +180,13 @@ __global__ void k_diag_partial(const double *__restrict__ rho, const double *__r
 // relax u toward (ub0, ub1), or toward the per-node target velocity (same
 // layout as u) when one is given
 __global__ void k_sponge(double *__restrict__ u, const double *__restrict__ alpha, double dt,
-                         double ub0, double ub1, const double *__restrict__ target, int nc,
-                         int nn2) {
+                         double ub0, double ub1, const double *__restrict__ target,
+                         const double *__restrict__ dts, int nc, int nn2) {
   const long n = (long)nc * nn2;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const double a = dt * alpha[i];
-    if (a == 0.0) continue;
     const long c = i / nn2, j = i - c * nn2;
+    const double a = dt * (dts ? dts[c] : 1.0) * alpha[i];
+    if (a == 0.0) continue;
     const long i0 = (c * 2) * nn2 + j, i1 = (c * 2 + 1) * nn2 + j;
     const double t0 = target ? target[i0] : ub0, t1 = target ? target[i1] : ub1;
     u[i0] = (u[i0] + a * t0) / (1.0 + a);
@@ -272,9 +272,9 @@ int vec_diagnostics(cudaStream_t st, const double *rho, const double *u, const d
   return ATM_OK;
 }
 int vec_sponge(cudaStream_t st, double *u, const double *alpha, double dt, double ub0,
-               double ub1, const double *target, int nc, int nn2) {
+               double ub1, const double *target, const double *dts, int nc, int nn2) {
   const long n = (long)nc * nn2;
-  k_sponge<<<grid_for(n), 256, 0, st>>>(u, alpha, dt, ub0, ub1, target, nc, nn2);
+  k_sponge<<<grid_for(n), 256, 0, st>>>(u, alpha, dt, ub0, ub1, target, dts, nc, nn2);
   ATM_CHECK_LAUNCH("k_sponge");
   return ATM_OK;
 }

@@ -282,7 +282,7 @@ MGHier<double> &hier<double>(MG &mg) { return mg.d; }
 template <typename T>
 void level_free(MGLevelT<T> &L) {
   cudaFree(L.mesh.qgeo); cudaFree(L.mesh.fgeo); cudaFree(L.mesh.nbr); cudaFree(L.mesh.nbrf);
-  cudaFree(L.mesh.hnb); cudaFree(L.mesh.hgeo);
+  cudaFree(L.mesh.hnb); cudaFree(L.mesh.hgeo); cudaFree(L.mesh.dts);
   cudaFree(L.parent); cudaFree(L.ppos); cudaFree(L.children);
   cudaFree(L.ainv); cudaFree(L.invd); cudaFree(L.rho); cudaFree(L.pfix);
   cudaFree(L.pfq); cudaFree(L.pff);
@@ -397,6 +397,25 @@ int build_hier(atm_ctx &c, MG &mg) {
       ATM_CUDA(cudaMemcpyAsync(F.ppos, ppos.data(), F.nc * sizeof(int), cudaMemcpyHostToDevice, c.stream));
       ATM_CUDA(cudaMemcpyAsync(H.lv[l].children, ch.data(), ch.size() * sizeof(int),
                                cudaMemcpyHostToDevice, c.stream));
+    }
+  }
+  if (c.mem) {
+    // each level cell carries its member's time-step multiplier (a merged
+    // cell's children belong to one member)
+    std::vector<double> prev(c.mem->dts_host);
+    for (size_t l = 0; l < nl; ++l) {
+      std::vector<T> cur(H.lv[l].nc);
+      if (l == 0) {
+        for (int i = 0; i < H.lv[0].nc; ++i) cur[i] = (T)prev[i];
+      } else {
+        std::vector<double> next(H.lv[l].nc);
+        for (int cc = 0; cc < H.lv[l].nc; ++cc) next[cc] = prev[mg.children[l][4 * cc]];
+        for (int i = 0; i < H.lv[l].nc; ++i) cur[i] = (T)next[i];
+        prev.swap(next);
+      }
+      ATM_CUDA(cudaMalloc(&H.lv[l].mesh.dts, cur.size() * sizeof(T)));
+      ATM_CUDA(cudaMemcpy(H.lv[l].mesh.dts, cur.data(), cur.size() * sizeof(T),
+                          cudaMemcpyHostToDevice));
     }
   }
   H.built = true;
@@ -660,6 +679,25 @@ int prepare_any(atm_ctx &c, int precision) {
 }
 
 }  // namespace
+
+int mg_prepare(atm_ctx &c, int precision) {
+  if (!c.mg || c.mg->hm.size() < 2) {
+    set_error("no multigrid levels (atm_mg_add_level)");
+    return ATM_NOT_READY;
+  }
+  return prepare_any(c, precision);
+}
+int mg_vcycle_only(atm_ctx &c, int precision, double *z, const double *v) {
+  return precision == 2 ? precondition<double>(c, *c.mg, z, v)
+                        : precondition<float>(c, *c.mg, z, v);
+}
+double *mg_zbasis(atm_ctx &c) { return c.mg ? c.mg->zbasis : nullptr; }
+int mg_restart(const atm_ctx &c) { return c.mg ? c.mg->restart : 16; }
+void mg_invalidate(atm_ctx &c) {
+  if (!c.mg) return;
+  hier_free(c.mg->f);
+  hier_free(c.mg->d);
+}
 
 // ------------------------------------------------------------- set-up --
 int mg_free(atm_ctx &c) {

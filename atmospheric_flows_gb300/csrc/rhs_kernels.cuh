@@ -44,6 +44,7 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
   __syncthreads();
   const bool active = lc < cnt;
   const int c = c0 + lc;
+  if (mesh.dts && active) co.dt *= mesh.dts[c];  // per-member time step
   double Sx[NN], Dx[NN];
   load_rows<K>(col, Sx, Dx);
   if (active) {
@@ -139,6 +140,7 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
   __syncthreads();
   const bool active = lc < cnt;
   const int c = c0 + lc;
+  if (mesh.dts && active) co.dt *= mesh.dts[c];  // per-member time step
   double Sx[NN], Dx[NN];
   load_rows<K>(col, Sx, Dx);
   const double dtM2 = co.dt / (co.Ma * co.Ma);
@@ -283,6 +285,7 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
   __syncthreads();
   const bool active = lc < cnt;
   const int c = c0 + lc;
+  if (mesh.dts && active) co.dt *= mesh.dts[c];  // per-member time step
   double Sx[NN], Dx[NN];
   load_rows<K>(col, Sx, Dx);
   const double M2 = co.Ma * co.Ma;

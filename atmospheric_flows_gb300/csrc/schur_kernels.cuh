@@ -35,6 +35,7 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
   __syncthreads();
   const bool active = lc < cnt;
   const int c = c0 + lc;
+  if (mesh.dts && active) cB *= mesh.dts[c];  // per-member time step
   T Sx[NN], Dx[NN];
   load_rows<K>(col, Sx, Dx);
   if (active) {
@@ -167,6 +168,7 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
   __syncthreads();
   const bool active = lc < cnt;
   const int c = c0 + lc;
+  if (mesh.dts && active) cC *= mesh.dts[c];  // per-member time step
   T Sx[NN], Dx[NN];
   load_rows<K>(col, Sx, Dx);
   if (active) {

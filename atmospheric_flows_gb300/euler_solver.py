@@ -30,7 +30,7 @@ class EulerSolver:
 
     def __init__(self, case, eps=1e-8, max_its=None, precision=0, dt=None, mg_levels=8,
                  true_residual_check=False, stream=None, levels=None, sponge_target=None,
-                 continue_on_not_converged=False):
+                 continue_on_not_converged=False, members=None):
         """`levels`: precomputed multigrid levels (default: the hill hierarchy of
         case.params); `sponge_target`: per-node sponge target velocity (batched
         members with different background winds).
@@ -39,7 +39,12 @@ class EulerSolver:
         ``AtmError`` (code NOT_CONVERGED) and leaves the state of the last
         completed step, as the reference's SolverControl throws
         (Atmospheric_Flow.cc:1289-1311); `continue_on_not_converged=True`
-        counts it in ``stats()["solve_fail"]`` and carries on instead."""
+        counts it in ``stats()["solve_fail"]`` and carries on instead.
+
+        `members` = (cell offsets, time steps): the case is several
+        independent members (batch.concat), each advanced with its own dt and
+        its own Krylov and Picard stops; :meth:`member_stats` reports each
+        member's outcome (a failed member does not stop the others)."""
         # Krylov iteration cap per Schur solve: the reference's GMRES cap for
         # precision 0; multigrid-preconditioned FGMRES needs tens, so a solve
         # that stalls gives up after 1000 instead of running for minutes
@@ -69,6 +74,15 @@ class EulerSolver:
                   int(max_its), int(precision))
         if continue_on_not_converged:
             _lib.call("atm_solver_set_continue_on_not_converged", self.op.handle, 1)
+        self.n_members = 0
+        if members is not None:
+            off = np.ascontiguousarray(members[0], dtype=np.int32)
+            dts = np.ascontiguousarray(members[1], dtype=np.float64)
+            if len(off) != len(dts) + 1:
+                raise ValueError("members: need len(offsets) == len(dts) + 1")
+            _lib.call("atm_set_members", self.op.handle, len(dts),
+                      off.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _d(dts))
+            self.n_members = len(dts)
         self.n_scalar = self.op.n_scalar
         self.set_state(case.rho, case.u, case.p)
         alpha = np.ascontiguousarray(case.sponge_alpha, dtype=np.float64)
@@ -99,6 +113,14 @@ class EulerSolver:
         keys = ("steps", "picard_total", "krylov_total", "picard_stage1", "picard_stage2",
                 "solve_fail", "time", "dt", "vcycles")
         return dict(zip(keys, s.tolist()))
+
+    def member_stats(self):
+        """Per member: status (0 ok, 2 not converged, 3 non-finite), Picard and
+        Krylov iterations, step of its failure (-1 none) and its dt."""
+        out = np.zeros(5 * self.n_members)
+        _lib.call("atm_member_stats", self.op.handle, self.n_members, _d(out))
+        keys = ("status", "picard", "krylov", "fail_step", "dt")
+        return [dict(zip(keys, out[5 * m:5 * m + 5].tolist())) for m in range(self.n_members)]
 
     def diagnostics(self):
         """The printouts of Atmospheric_Flow.cc:1121-1122,1225-1235 for the

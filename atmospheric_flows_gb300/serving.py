@@ -12,15 +12,19 @@ under continuous batching:
     join as soon as memory frees up;
   * members advance with the mixed-precision solver (FP64 state, FGMRES
     with an FP32 multigrid preconditioner) unless told otherwise;
-  * with batch_size > 1, requests waiting at admission that share mesh size,
-    degree and solver are concatenated into one context (batch.py): every
-    kernel launch then covers all of their cells.  A batch runs until its
-    longest member is done; each member's result is taken when its own step
-    count is reached.
+  * with batch_size > 1, requests waiting at admission that share the
+    degree and the solver (any mesh sizes) are concatenated into one context
+    (batch.py): every kernel launch then covers all of their cells, while
+    each member keeps its own time step and its own Krylov and Picard stops.
+    A batch runs until its longest member is done; each member's result is
+    taken when its own step count is reached, and a member that fails is
+    reported alone.
 
-Members never share device data or reductions, so a member's result is the
-same alone and in a mix (the kernels are deterministic).  The reference has
-no serving loop; it runs one member per MPI job (Atmospheric_Flow.cc:1265-1313).
+Unbatched members never share device data or reductions, so a member's
+result is bitwise the same alone and in a mix (the kernels are
+deterministic); a batched member matches its solo run to the solver
+tolerance.  The reference has no serving loop; it runs one member per MPI
+job (Atmospheric_Flow.cc:1265-1313).
 """
 from __future__ import annotations
 
@@ -176,6 +180,7 @@ class Server:
         n = len(reqs)
         finished = [None] * n
         states = [None] * n
+        statuses = ["ok"] * n
         status = "ok"
         stream = ctypes.c_void_p()
         solver = None
@@ -189,18 +194,25 @@ class Server:
             solver = EulerSolver(b.case, eps=reqs[0].eps, precision=prec,
                                  true_residual_check=prec != 0, stream=stream.value,
                                  levels=b.levels if prec != 0 else None,
-                                 sponge_target=b.u_target)
+                                 sponge_target=b.u_target, members=(b.offsets, b.dts))
             if any(r.initial_state is not None for r in reqs):
                 parts = [r.initial_state if r.initial_state is not None else (c.rho, c.u, c.p)
                          for r, c in zip(reqs, cases)]
                 solver.set_state(*(np.concatenate([q[f] for q in parts]) for f in range(3)))
             target = [r.steps for r in reqs]
             steps = 0
-            while steps < max(target):
-                nxt = min(t for t in target if t > steps)
+            while any(f is None for f in finished):
+                nxt = min(target[i] for i in range(n) if finished[i] is None)
                 k = min(self.chunk, nxt - steps)
                 solver.run(k)
                 steps += k
+                mst = solver.member_stats()
+                for i in range(n):
+                    if finished[i] is None and mst[i]["status"] != 0:
+                        code = _lib.STATUS.get(int(mst[i]["status"]), mst[i]["status"])
+                        statuses[i] = (f"error: member failed at step {int(mst[i]['fail_step'])}"
+                                       f": {code}")
+                        finished[i] = time.perf_counter() - t0
                 due = [i for i in range(n) if finished[i] is None and target[i] <= steps]
                 if due:
                     parts = b.split_state(solver.get_state()) if self.keep_state else None
@@ -226,7 +238,7 @@ class Server:
                     self.results.append(MemberResult(
                         r.request_id, r.arrival, admitted,
                         finished[i] if finished[i] is not None else end, r.steps, dofs[i],
-                        status, states[i]))
+                        status if status != "ok" else statuses[i], states[i]))
                 self._lock.notify_all()
 
     def run(self, requests, time_scale=1.0):

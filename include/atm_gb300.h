@@ -292,6 +292,26 @@ int atm_solver_run(atm_handle h, int n_steps);
  * step carries on with the unconverged iterate; on = 0 (default): it fails
  * as atm_solver_run says.  No reference counterpart (deal.II always throws). */
 int atm_solver_set_continue_on_not_converged(atm_handle h, int on);
+/* ---------------------------------------------------------------------------
+ * Several independent members in one context (ensemble serving).  No
+ * reference counterpart: the reference runs one member per process
+ * (Atmospheric_Flow.cc:1265-1313).  The context's cells are n_members
+ * contiguous ranges cell_offsets[m] .. cell_offsets[m+1] (n_members + 1
+ * entries, from 0 to n_cells) that share no faces, and member m advances with
+ * its own time step member_dt[m] (the context's dt only sets the units).
+ * Every Schur solve and Picard loop is then member-wise: inner products,
+ * Krylov stops and Picard stops are each member's own, so a member's result
+ * does not depend on the others in the context.  A member whose solve fails
+ * (non-converged, or a non-finite state or residual) is frozen at a uniform
+ * rest state and reported by atm_member_stats; the others carry on and
+ * atm_solver_run returns ATM_OK.  Multigrid levels must keep members apart
+ * (each coarse cell's children in one member).  n_members = 0 returns to a
+ * single member.  Call after atm_solver_init. */
+int atm_set_members(atm_handle h, int n_members, const int *cell_offsets,
+                    const double *member_dt);
+/* out[5 m + 0..4] for each member m: status (ATM_OK or its failure), Picard
+ * iterations, Krylov iterations, step of its failure (-1: none), its dt. */
+int atm_member_stats(atm_handle h, int n, double *out);
 /* stats[0..8] as doubles: steps, Picard iterations (total), Krylov
  * iterations (total), last Picard count stage 1, stage 2, Krylov solves that
  * hit max_its, simulated time, current dt, V-cycles (total). */

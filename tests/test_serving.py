@@ -61,61 +61,111 @@ def test_server_budget_and_latency(cuda_ok):
     assert s["aggregate_dof_steps_per_s"] > 0
 
 
-def _batch_cases():
+def _mixed_batch_cases():
     from atmospheric_flows_gb300.hill import build_case
 
-    return [build_case(HillParams(nx=16, nz=8, degree=3, h0=h, u0=u, seed=s, theta_noise=0.1))
-            for h, u, s in ((300.0, 8.0, 1), (450.0, 12.0, 2), (200.0, 6.0, 3))]
+    return [build_case(HillParams(nx=nx, nz=nz, degree=3, h0=h, u0=u, seed=s, theta_noise=0.1,
+                                  cfl=cfl))
+            for nx, nz, h, u, s, cfl in ((16, 8, 300.0, 8.0, 1, 4.0), (32, 16, 450.0, 12.0, 2, 5.0),
+                                         (8, 4, 200.0, 6.0, 3, 3.0))]
 
 
 def test_batch_tables_are_block_diagonal():
+    """Members of different meshes concatenate into disconnected cell ranges;
+    each keeps its own dt and wind; the multigrid levels keep members apart,
+    and a member whose hierarchy is shallower keeps its coarsest level on
+    the deeper levels (rows (cell, -1, -1, -1))."""
     from atmospheric_flows_gb300 import batch
 
-    cases = _batch_cases()
+    cases = _mixed_batch_cases()
     b = batch.concat(cases)
-    nc = cases[0].n_cells
-    assert b.case.n_cells == 3 * nc and b.offsets == [0, nc, 2 * nc]
-    assert b.case.dt == min(c.dt for c in cases)
-    member = lambda cell: cell // nc  # noqa: E731
+    off = b.offsets
+    assert off == [0, 128, 128 + 512, 128 + 512 + 32]
+    assert b.dts == [c.dt for c in cases] and len(set(b.dts)) == 3
+    member = lambda cell: np.searchsorted(off, cell, side="right") - 1  # noqa: E731
     inner = b.case.inner_faces
     assert np.all(member(inner[:, 0]) == member(inner[:, 2]))
-    assert len(inner) == 3 * len(cases[0].inner_faces)
-    assert len(b.case.boundary_faces) == 3 * len(cases[0].boundary_faces)
-    prev = nc
+    assert len(inner) == sum(len(c.inner_faces) for c in cases)
+    prev_off = off
     for lv in b.levels:
-        m = lv["n_cells"] // 3
         ch = lv["children"]
-        assert sorted(ch.ravel().tolist()) == list(range(3 * prev))
-        assert np.all(ch // prev == (np.arange(3 * m) // m)[:, None])
-        prev = m
-    tgt = b.u_target.reshape(3 * nc, 2, -1)
-    assert np.all(tgt[:nc, 0] == 8.0) and np.all(tgt[nc:2 * nc, 0] == 12.0)
+        same = np.all(ch[:, 1:] < 0, axis=1)
+        cells = np.concatenate([ch[same, 0], ch[~same].ravel()])
+        assert sorted(cells.tolist()) == list(range(prev_off[-1]))
+        # every row's cells lie in one member of the finer level
+        pm = np.searchsorted(prev_off, ch[:, 0], side="right") - 1
+        for q in range(1, 4):
+            sel = ch[:, q] >= 0
+            assert np.all(np.searchsorted(prev_off, ch[sel, q], side="right") - 1 == pm[sel])
+        counts = np.bincount(pm, minlength=3)
+        prev_off = [0] + np.cumsum(counts).tolist()
+    # the 8x4 member reaches its coarsest level first and is carried along
+    assert any(np.all(lv["children"][:, 1:] < 0, axis=1).any() for lv in b.levels)
+    tgt = b.u_target.reshape(off[-1], 2, -1)
+    assert np.all(tgt[:128, 0] == 8.0) and np.all(tgt[128:640, 0] == 12.0)
     assert np.all(tgt[:, 1] == 0.0)
     rho = b.split(b.case.rho)
     assert all(np.array_equal(r, c.rho) for r, c in zip(rho, cases))
 
 
 @pytest.mark.gpu
-def test_member_same_alone_and_in_batch(cuda_ok):
+@pytest.mark.parametrize("precision,eps,bar", [(0, 1e-10, 1e-9), (1, 1e-11, 1e-8)])
+def test_member_same_alone_and_in_batch(cuda_ok, precision, eps, bar):
+    """Three members of different meshes and time steps in one context: each
+    matches its solo run at its own dt -- GMRES + Jacobi to 1e-9, FGMRES +
+    FP32 multigrid to 1e-8 relative L2 per field (the batch's V-cycle uses
+    the batch's Chebyshev interval, so the preconditioner differs)."""
     from atmospheric_flows_gb300 import batch
     from atmospheric_flows_gb300.euler_solver import EulerSolver
 
-    cases = _batch_cases()
+    cases = _mixed_batch_cases()
     b = batch.concat(cases)
-    kw = dict(eps=1e-10, precision=1, true_residual_check=True)
-    g = EulerSolver(b.case, levels=b.levels, sponge_target=b.u_target, **kw)
+    kw = dict(eps=eps, precision=precision, true_residual_check=precision != 0)
+    g = EulerSolver(b.case, levels=b.levels if precision else None, sponge_target=b.u_target,
+                    members=(b.offsets, b.dts), **kw)
     g.run(3)
     parts = b.split_state(g.get_state())
+    ms = g.member_stats()
     g.close()
+    assert [m["status"] for m in ms] == [0, 0, 0]
     for i, c in enumerate(cases):
-        s = EulerSolver(c, dt=b.case.dt, **kw)
+        s = EulerSolver(c, **kw)
         s.run(3)
-        # the batch's shared Krylov stop and Picard loop (every member
-        # iterates until all converge) move each member by the solver
-        # tolerance, amplified into u by dt/Ma^2: measured 1.0e-8 in u
+        st = s.stats()
         for a, ref in zip(parts[i], s.get_state()):
-            assert np.linalg.norm(a - ref) / np.linalg.norm(ref) < 1e-7
+            assert np.linalg.norm(a - ref) / np.linalg.norm(ref) < bar
+        if precision == 0:
+            assert ms[i]["picard"] == st["picard_total"]
         s.close()
+
+
+@pytest.mark.gpu
+def test_poisoned_member_fails_alone_in_batch(cuda_ok):
+    """A batched member whose state holds a NaN fails alone (NONFINITE, at
+    step 1); the other members of the same context are bitwise what they are
+    beside a clean member."""
+    from atmospheric_flows_gb300 import batch
+    from atmospheric_flows_gb300.euler_solver import EulerSolver
+
+    cases = _mixed_batch_cases()
+    b = batch.concat(cases)
+    out = []
+    for poison in (False, True):
+        g = EulerSolver(b.case, eps=1e-10, sponge_target=b.u_target, members=(b.offsets, b.dts))
+        rho = b.case.rho.copy()
+        if poison:
+            rho[b.offsets[1] * 16 + 7] = np.nan
+        g.set_state(rho, b.case.u, b.case.p)
+        g.run(2)
+        out.append((b.split_state(g.get_state()), g.member_stats()))
+        g.close()
+    (clean, s0), (mixed, s1) = out
+    assert [m["status"] for m in s0] == [0, 0, 0]
+    assert s1[1]["status"] == 3 and s1[1]["fail_step"] == 1
+    for i in (0, 2):
+        assert s1[i]["status"] == 0
+        for a, ref in zip(mixed[i], clean[i]):
+            assert np.array_equal(a, ref)
 
 
 @pytest.mark.gpu
