@@ -59,6 +59,8 @@ def parse():
                          "200 steps, 1e-10 drifts to ~1.1e-8-1.9e-8 in u")
     ap.add_argument("--precision", default="fp64", choices=["fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving-sample", action="store_true",
+                    help="leave the bounded serving sample out of the main line")
     ap.add_argument("--only-headline", action="store_true",
                     help="skip the multigrid variants (short runs, profiling)")
     ap.add_argument("--serving", action="store_true",
@@ -509,6 +511,12 @@ def run_gb300(args):
         except Exception as exc:  # the baseline must not kill the GPU line
             cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port",
                    "sample": f"failed: {exc}"}
+    serving_sub = None
+    if not args.only_headline and not args.no_serving_sample:
+        try:
+            serving_sub = serving_sample()
+        except Exception as exc:  # the sample must not kill the GPU line
+            serving_sub = {"note": f"failed: {exc}"}
     st = main["stats"]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": main["el_ms"] / args.steps,
@@ -527,10 +535,32 @@ def run_gb300(args):
                        "krylov_per_step": st["krylov_total"] / max(st["steps"], 1),
                        "solve_fail": st["solve_fail"]},
             **variants}
+    if serving_sub is not None:
+        line["serving"] = serving_sub
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def serving_sample():
+    """A bounded sample of the ensemble-serving workload for the main line:
+    16 Poisson requests at 4/s, meshes 40x20 and 80x40, degrees 2-3, 100-400
+    steps scaled by 0.1, mixed-precision solver, batches of up to 4 waiting
+    requests (member-wise solves).  p50/p95/p99 latency and aggregate
+    DoF-steps/s."""
+    from atmospheric_flows_gb300.serving import Server, make_requests, summarize
+
+    reqs = make_requests(n=16, rate=4.0, seed=0, steps_scale=0.1, meshes=((40, 20), (80, 40)),
+                         degrees=(2, 3))
+    srv = Server(hbm_budget=150e9, max_running=32, batch_size=4)
+    res = srv.run(reqs)
+    out = summarize(res, srv.makespan)
+    out.update({"sample": "16 requests, Poisson 4/s, meshes 40x20/80x40, k 2-3, steps 100-400 "
+                          "x 0.1, FGMRES + FP32 multigrid rtol 1e-8, batches of up to 4",
+                "batches": len(srv.batches),
+                "members_per_batch_mean": float(np.mean(srv.batches)) if srv.batches else 0.0})
+    return out
 
 
 def fma_probe():
