@@ -538,7 +538,7 @@ class AdaptiveMember:
         # after every adaptation; stop on the true residual (S is nonlinear)
         return self._Solver(self.case, eps=self.eps, precision=self.precision, dt=self.dt,
                             stream=self.stream, true_residual_check=True,
-                            levels=mg_hierarchy_adaptive(self.p, self.tree))
+                            levels=mg_hierarchy_adaptive(self.p, self.tree, max_levels=3))
 
     def _adapt_state(self, rho, u, pres):
         k, m = self.p.degree, self.p.mapping_degree

@@ -64,7 +64,7 @@ def _offset_faces(inner, bdry, off):
     return inner, bdry
 
 
-def concat(cases, mg_levels: int = 8) -> Batch:
+def concat(cases, mg_levels: int = 3) -> Batch:
     """Concatenate members (same batch_key; any mesh sizes) into one case."""
     if not cases:
         raise ValueError("empty batch")

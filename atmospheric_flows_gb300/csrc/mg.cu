@@ -75,7 +75,7 @@ struct MG {
   int cheb_deg = 3;
   double range = 15.0;
   int eig_its = 10;
-  int coarse_deg = 20;
+  int coarse_deg = 10;
   double coarse_range = 50.0;
   int restart = 16;
   double *zbasis = nullptr;  // FGMRES preconditioned directions [restart][ns]

@@ -32,20 +32,6 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
   const int c0 = blockIdx.x * CPB;
   const int cnt = min(CPB, mesh.nc - c0);
   load_tiles<K>(tiles, NT, 0, p, 1, c0, cnt);
-  // FP32 (multigrid levels) is bound by memory latency, not by arithmetic:
-  // this column's geometry loads go out before the barrier, all at once,
-  // so they overlap the tile load and each other
-  constexpr bool PRE = sizeof(T) == 4;
-  T gq[PRE ? 4 : 1][PRE ? NQ : 1];
-  if constexpr (PRE) {
-    if (lc < cnt) {
-      const T *G = mesh.qgeo + (long)(c0 + lc) * 5 * NQ2 + col;
-#pragma unroll
-      for (int f = 0; f < 4; ++f)
-#pragma unroll
-        for (int qz = 0; qz < NQ; ++qz) gq[f][qz] = G[f * NQ2 + qz * NQ];
-    }
-  }
   __syncthreads();
   const bool active = lc < cnt;
   const int c = c0 + lc;
@@ -63,18 +49,10 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     for (int comp = 0; comp < 2; ++comp) {
 #pragma unroll
       for (int qz = 0; qz < NQ; ++qz) {
-        T gxi, get;
-        if constexpr (PRE) {
-          gxi = gq[comp][qz];      // xx or xz
-          get = gq[2 + comp][qz];  // ex or ez
-        } else {
-          const auto g = qgeo<K>(G, qz * NQ + col);
-          gxi = comp == 0 ? g.xx : g.xz;
-          get = comp == 0 ? g.ex : g.ez;
-        }
+        const auto g = qgeo<K>(G, qz * NQ + col);
         const T s = -cB * pv[qz];
-        Gxi[qz] = gxi * s;
-        Get[qz] = get * s;
+        Gxi[qz] = (comp == 0 ? g.xx : g.xz) * s;
+        Get[qz] = (comp == 0 ? g.ex : g.ez) * s;
         V[qz] = T(0.0);
       }
       T *xa = xab + (lc * 2 + comp) * 2 * NN * NQ;
@@ -187,24 +165,6 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
   load_tiles<K>(tiles, NT, 0, w, 2, c0, cnt);
   if (HG) load_tiles<K>(tiles, NT, 2, pfix, 1, c0, cnt);
   if (WITH_D) load_tiles<K>(tiles, NT, TP, p, 1, c0, cnt);
-  // FP32 (multigrid levels): geometry and prepared p_fix of this column are
-  // loaded before the barrier, all at once (latency bound, as in k_B)
-  constexpr bool PRE = sizeof(T) == 4;
-  constexpr int NG = WITH_D ? 5 : 4;
-  T gq[PRE ? NG : 1][PRE ? NQ : 1], pq[PRE ? NQ : 1];
-  if constexpr (PRE) {
-    if (lc < cnt) {
-      const T *G = mesh.qgeo + (long)(c0 + lc) * 5 * NQ2 + col;
-#pragma unroll
-      for (int f = 0; f < NG; ++f)
-#pragma unroll
-        for (int qz = 0; qz < NQ; ++qz) gq[f][qz] = G[f * NQ2 + qz * NQ];
-      if (!HG) {
-#pragma unroll
-        for (int qz = 0; qz < NQ; ++qz) pq[qz] = pfq[(long)(c0 + lc) * NQ2 + qz * NQ + col];
-      }
-    }
-  }
   __syncthreads();
   const bool active = lc < cnt;
   const int c = c0 + lc;
@@ -220,23 +180,14 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
       eval_col<K>(tl + 2 * NN2, Sx, pf);
     } else {
 #pragma unroll
-      for (int qz = 0; qz < NQ; ++qz) {
-        if constexpr (PRE) pf[qz] = pq[qz];
-        else pf[qz] = pfq[(long)c * NQ2 + qz * NQ + col];
-      }
+      for (int qz = 0; qz < NQ; ++qz) pf[qz] = pfq[(long)c * NQ2 + qz * NQ + col];
     }
     if (WITH_D) eval_col<K>(tl + TP * NN2, Sx, pv);
     const T *G = mesh.qgeo + (long)c * 5 * NQ2;
     T V[NQ], Gxi[NQ], Get[NQ];
 #pragma unroll
     for (int qz = 0; qz < NQ; ++qz) {
-      QGeoT<T> g;
-      if constexpr (PRE) {
-        g.xx = gq[0][qz]; g.xz = gq[1][qz]; g.ex = gq[2][qz]; g.ez = gq[3][qz];
-        g.jxw = gq[NG - 1][qz];  // read only when WITH_D (then NG = 5)
-      } else {
-        g = qgeo<K>(G, qz * NQ + col);
-      }
+      const auto g = qgeo<K>(G, qz * NQ + col);
       // C: submit_gradient(-cC hg pfix w)
       const T gx = SC * (-cC * HG_ * pf[qz] * wx[qz]);
       const T gz = SC * (-cC * HG_ * pf[qz] * wz[qz]);

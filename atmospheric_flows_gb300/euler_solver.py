@@ -28,7 +28,7 @@ class EulerSolver:
     PRECISION_MIXED = 1   # FGMRES + FP32 multigrid V-cycle
     PRECISION_FP64_MG = 2  # FGMRES + FP64 multigrid V-cycle
 
-    def __init__(self, case, eps=1e-8, max_its=None, precision=0, dt=None, mg_levels=8,
+    def __init__(self, case, eps=1e-8, max_its=None, precision=0, dt=None, mg_levels=3,
                  true_residual_check=False, stream=None, levels=None, sponge_target=None,
                  continue_on_not_converged=False, members=None):
         """`levels`: precomputed multigrid levels (default: the hill hierarchy of

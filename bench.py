@@ -87,6 +87,12 @@ def parse():
     ap.add_argument("--amr-precision", type=int, default=1, choices=[0, 1, 2],
                     help="Schur solver of the adaptive sample: 0 the reference's GMRES + "
                          "Jacobi, 1 FP32 multigrid (default), 2 FP64 multigrid")
+    ap.add_argument("--vcycle", action="store_true",
+                    help="time the multigrid V-cycle of the workload alone and exit")
+    ap.add_argument("--vcycle-no-graphs", action="store_true")
+    ap.add_argument("--vcycle-fp64", action="store_true")
+    ap.add_argument("--mg-levels", type=int, default=3)
+    ap.add_argument("--mg-coarse-degree", type=int, default=10)
     ap.add_argument("--fma-probe", action="store_true",
                     help="print the measured FP64/FP32 FMA peaks and exit")
     return ap.parse_args()
@@ -563,6 +569,64 @@ def serving_sample():
     return out
 
 
+def vcycle_sample(args):
+    """Time the multigrid V-cycle of the workload alone: the Schur operator of
+    IMEX stage 1 with rho_fix and p_fix perturbed by 1e-3, `--warmup`
+    V-cycles, then `--steps` timed ones (CUDA events), launched kernel by
+    kernel with `--vcycle-no-graphs` (for per-launch profiles) or replayed as
+    a captured graph.  Prints ms per V-cycle and the residual reduction of one
+    V-cycle on S x = b for a random x."""
+    import torch
+
+    torch.cuda.set_device(0)
+    from atmospheric_flows_gb300.euler_operator import EULEROperator, MatrixFreeStorage
+    from atmospheric_flows_gb300.hill import HillParams, build_case, mg_hierarchy
+
+    case = build_case(HillParams(nx=args.nx, nz=args.nz, degree=args.degree, cfl=args.cfl))
+    op = EULEROperator(MatrixFreeStorage.from_case(case), case.dt, case.Ma, case.Fr)
+    levels = mg_hierarchy(case.params, max_levels=args.mg_levels)
+    for lv in levels:
+        op.add_mg_level(lv)
+    op.set_mg_smoother(coarse_degree=args.mg_coarse_degree)
+    rng = np.random.default_rng(3)
+
+    def dev(a):
+        return torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+
+    op.set_rho_for_fixed(dev(case.rho * (1 + 1e-3 * rng.standard_normal(case.rho.shape))))
+    op.set_pres_fixed(dev(case.p * (1 + 1e-3 * rng.standard_normal(case.p.shape))))
+    op.set_HYPERBOLIC_stage(1)
+    op.set_NS_stage(2)
+    op.set_mg_graphs(not args.vcycle_no_graphs)
+    prec = 2 if args.vcycle_fp64 else 1
+    x = dev(rng.standard_normal(op.n_scalar))
+    b = torch.empty_like(x)
+    op.vmult(b, x)
+    z = torch.empty_like(x)
+    for _ in range(args.warmup):
+        op.mg_vcycle(z, b, prec)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        op.mg_vcycle(z, b, prec)
+    e1.record()
+    torch.cuda.synchronize()
+    r = torch.empty_like(x)
+    op.vmult(r, z)
+    print(json.dumps({"metric": "multigrid V-cycle time", "unit": "ms",
+                      "value": e0.elapsed_time(e1) / args.steps,
+                      "precision": "fp64" if prec == 2 else "fp32",
+                      "graphs": not args.vcycle_no_graphs, "levels": len(levels) + 1,
+                      "max_levels": args.mg_levels, "coarse_degree": args.mg_coarse_degree,
+                      "residual_reduction": ((b - r).norm() / b.norm()).item(),
+                      "config": {"workload": f"Schur operator of {args.nx}x{args.nz} "
+                                             f"Q{args.degree}"}}), flush=True)
+    op.close()
+    return 0
+
+
 def fma_probe():
     import torch
 
@@ -780,6 +844,8 @@ def main():
     args = parse()
     if args.fma_probe:
         return fma_probe()
+    if args.vcycle:
+        return vcycle_sample(args)
     if args.serving_compare:
         return serving_compare(args)
     if args.serving_rates:
