@@ -78,7 +78,7 @@ def test_batch_tables_are_block_diagonal():
     from atmospheric_flows_gb300 import batch
 
     cases = _mixed_batch_cases()
-    b = batch.concat(cases)
+    b = batch.concat(cases, mg_levels=8)
     off = b.offsets
     assert off == [0, 128, 128 + 512, 128 + 512 + 32]
     assert b.dts == [c.dt for c in cases] and len(set(b.dts)) == 3
@@ -119,8 +119,9 @@ def test_member_same_alone_and_in_batch(cuda_ok, precision, eps, bar):
     from atmospheric_flows_gb300.euler_solver import EulerSolver
 
     cases = _mixed_batch_cases()
-    b = batch.concat(cases)
-    kw = dict(eps=eps, precision=precision, true_residual_check=precision != 0)
+    # 5 levels: the 8x4 member's hierarchy (3 levels) is padded on the deeper ones
+    b = batch.concat(cases, mg_levels=5)
+    kw = dict(eps=eps, precision=precision, true_residual_check=precision != 0, mg_levels=5)
     g = EulerSolver(b.case, levels=b.levels if precision else None, sponge_target=b.u_target,
                     members=(b.offsets, b.dts), **kw)
     g.run(3)
