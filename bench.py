@@ -695,6 +695,7 @@ def serving_sweep(args):
         rows.append({"rate_per_s": rate, "last_arrival_s": last, **{k: s[k] for k in (
             "completed", "p50_latency_s", "p95_latency_s", "p99_latency_s", "mean_queue_wait_s",
             "aggregate_dof_steps_per_s", "makespan_s")}})
+        print(json.dumps(rows[-1]), file=sys.stderr, flush=True)  # partial progress
     rows.sort(key=lambda r: r["rate_per_s"])
     ref_p99 = rows[0]["p99_latency_s"]
     kept = [r for r in rows if r["completed"] == args.serving_requests
