@@ -73,6 +73,18 @@ SIGNATURES = {
     "atm_solver_run": (_i, [_h, _i]),
     "atm_solver_set_continue_on_not_converged": (_i, [_h, _i]),
     "atm_solver_stats": (_i, [_h, _dp]),
+    "atm3_ctx_create": (_i, [_i, _dp, _i, _ip, _ip, _i, _ip, ctypes.POINTER(_h)]),
+    "atm3_ctx_destroy": (_i, [_h]),
+    "atm3_set_params": (_i, [_h, _d, _d, _d]),
+    "atm3_set_stage": (_i, [_h, _i, _i]),
+    "atm3_set_frozen": (_i, [_h, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "atm3_rhs": (_i, [_h, _i, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), _i]),
+    "atm3_apply": (_i, [_h, _i, ctypes.c_void_p, ctypes.c_void_p]),
+    "atm3_solver_init": (_i, [_h, _d, _i, _i, _i]),
+    "atm3_solver_set_state": (_i, [_h, _dp, _dp, _dp]),
+    "atm3_solver_get_state": (_i, [_h, _dp, _dp, _dp]),
+    "atm3_solver_run": (_i, [_h, _i]),
+    "atm3_solver_stats": (_i, [_h, _dp]),
     "atm_set_members": (_i, [_h, _i, ctypes.POINTER(ctypes.c_int), _dp]),
     "atm_member_stats": (_i, [_h, _i, _dp]),
     "atm_solver_diagnostics": (_i, [_h, _dp]),

@@ -320,6 +320,54 @@ int atm_solver_stats(atm_handle h, double *stats);
  * out[0..3] = min rho, max |rho|, max sqrt(gamma p/rho), max |u|. */
 int atm_solver_diagnostics(atm_handle h, double *out);
 
+/* ---------------------------------------------------------------------------
+ * The reference's own 3D case: FE_DGQ(1) hexahedra on a spherical shell with
+ * radial gravity -e_r a^2/r^2 / Fr^2 (EulerSolver<3>, Atmospheric_Flow.cc:
+ * 279-286, 1277; euler_operator.h:790-811 for the gravity terms).  Same
+ * operators, stages and time loop as the 2D entry points above, dim = 3.
+ *   mapping_nodes : [n_cells][27][3] host, degree-2 mapping (MappingQ(2),
+ *                   equation_data.h:43) at the points {0, 1/2, 1}^3, first
+ *                   reference coordinate fastest; right-handed cells
+ *   inner_faces   : [n_inner][4] host: cell+, face+, cell-, face- (local faces
+ *                   0/1: xi1 = 0/1, 2/3: xi2, 4/5: xi3)
+ *   face_perm     : [n_inner][9] host: the 3x3 Gauss points of face+ (lower
+ *                   tangential coordinate fastest) are, in order, the points
+ *                   face_perm[q] of face- (rotated or flipped neighbours)
+ *   bdry_faces    : [n_bdry][3] host: cell, face, id (walls)
+ * Fields: scalars [cell][8], velocity [cell][3][8] on the cell vertices.
+ * ------------------------------------------------------------------------- */
+typedef struct atm3_ctx *atm3_handle;
+int atm3_ctx_create(int n_cells, const double *mapping_nodes, int n_inner,
+                    const int *inner_faces, const int *face_perm, int n_bdry,
+                    const int *bdry_faces, atm3_handle *out);
+int atm3_ctx_destroy(atm3_handle h);
+/* set_dt / set_Mach / set_Froude, set_HYPERBOLIC_stage / set_NS_stage
+ * (euler_operator.h:34-43). */
+int atm3_set_params(atm3_handle h, double dt, double mach, double froude);
+int atm3_set_stage(atm3_handle h, int hyperbolic_stage, int ns_stage);
+/* set_rho_for_fixed / set_pres_fixed / set_u_fixed (euler_operator.h:45-52),
+ * device pointers, NULL leaves a field unchanged; rho rebuilds A^{-1}. */
+int atm3_set_frozen(atm3_handle h, const double *rho, const double *pres, const double *u);
+/* which 0/1/2: vmult_rhs_rho_update / vmult_rhs_velocity_fixed /
+ * vmult_rhs_pressure (euler_operator.h:54-61), positional sources as the 2D
+ * entry points; device pointers, dst overwritten. */
+int atm3_rhs(atm3_handle h, int which, double *dst, const double *const *src, int nsrc);
+/* which 0: vmult_pressure (B), 1: vmult_enthalpy (C), 2: Base::vmult of the
+ * current NS stage (euler_operator.h:63-65, 93, 2366-2417). */
+int atm3_apply(atm3_handle h, int which, double *dst, const double *src);
+/* EulerSolver (Atmospheric_Flow.cc:430-871, 1100-1257) with GMRES + Jacobi for
+ * the Schur system.  scaled_tol = 0 stops as the reference, eps |rhs| on the
+ * Jacobi-scaled residual; on the shell diag(D)^{-1} ~ 1/|cell| is tiny and
+ * that rule stops before the first iteration, so scaled_tol = 1 compares with
+ * eps |diag(D)^{-1} rhs| instead.  State with HOST pointers. */
+int atm3_solver_init(atm3_handle h, double eps, int max_its, int scaled_tol,
+                     int true_residual_check);
+int atm3_solver_set_state(atm3_handle h, const double *rho, const double *u, const double *p);
+int atm3_solver_get_state(atm3_handle h, double *rho, double *u, double *p);
+int atm3_solver_run(atm3_handle h, int n_steps);
+/* out[0..3]: steps, Picard iterations, Krylov iterations, solves that hit max_its. */
+int atm3_solver_stats(atm3_handle h, double *out);
+
 #ifdef __cplusplus
 }
 #endif

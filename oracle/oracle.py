@@ -255,3 +255,106 @@ class OracleSolver:
 
 def num_threads() -> int:
     return lib().orc_num_threads()
+
+
+# ---------------------------------------------------------------- 3D shell --
+_SHELL = os.path.join(_HERE, "liboracle_shell.so")
+_shell = None
+
+
+def build_shell(force: bool = False) -> str:
+    """Compile the 3D shell oracle (shell_oracle.cpp) with the Makefile."""
+    src = os.path.join(_HERE, "shell_oracle.cpp")
+    if force or not os.path.exists(_SHELL) or os.path.getmtime(_SHELL) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", _HERE, "-B", "liboracle_shell.so"], check=True)
+    return _SHELL
+
+
+def shell_lib():
+    global _shell
+    if _shell is None:
+        build_shell()
+        L = ctypes.CDLL(_SHELL)
+        L.orc3_create.restype = ctypes.c_void_p
+        L.orc3_create.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _ip, _ip, ctypes.c_int, _ip,
+                                  ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                  ctypes.c_double]
+        L.orc3_destroy.argtypes = [ctypes.c_void_p]
+        L.orc3_set_tolerances.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_int]
+        L.orc3_set_stage.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.orc3_set_frozen.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+        L.orc3_rhs.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, ctypes.POINTER(_dp)]
+        L.orc3_apply.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
+        L.orc3_set_state.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+        L.orc3_get_state.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+        L.orc3_run.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc3_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_long)]
+        _shell = L
+    return _shell
+
+
+class OracleShell:
+    """CPU restatement of EULEROperator + EulerSolver in 3D (FE_DGQ(1)) on the
+    spherical shell (shell_oracle.cpp); `case` is a shell.ShellCase."""
+
+    def __init__(self, case, eps=1e-8, inner_tol=1e-12, max_its=30000,
+                 true_residual_check=False, scaled_tol=False):
+        L = shell_lib()
+        self.case = case
+        self._keep = [np.ascontiguousarray(case.mapping_nodes, dtype=np.float64),
+                      np.ascontiguousarray(case.inner_faces, dtype=np.int32),
+                      np.ascontiguousarray(case.face_perm, dtype=np.int32),
+                      np.ascontiguousarray(case.boundary_faces, dtype=np.int32)]
+        nodes, inner, perm, bdry = self._keep
+        self.h = L.orc3_create(case.n_cells, _d(nodes), len(inner), _i(inner), _i(perm),
+                               len(bdry), _i(bdry), case.dt, case.Ma, case.Fr, eps)
+        L.orc3_set_tolerances(self.h, inner_tol, int(bool(true_residual_check)), max_its,
+                              int(bool(scaled_tol)))
+        self.ns = case.n_cells * 8
+        self.set_state(case.rho, case.u, case.p)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            shell_lib().orc3_destroy(self.h)
+            self.h = None
+
+    def set_stage(self, hyperbolic_stage, ns_stage):
+        shell_lib().orc3_set_stage(self.h, hyperbolic_stage, ns_stage)
+
+    def set_frozen(self, rho=None, p=None, u=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+                for a in (rho, p, u)]
+        shell_lib().orc3_set_frozen(self.h, *[None if a is None else _d(a) for a in arrs])
+
+    def rhs(self, which, src):
+        """which: 0 rho, 1 momentum, 2 energy; src: the positional source list."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in src]
+        ptrs = (_dp * len(arrs))(*[_d(a) for a in arrs])
+        dst = np.zeros(self.ns * (3 if which == 1 else 1))
+        shell_lib().orc3_rhs(self.h, which, _d(dst), ptrs)
+        return dst
+
+    def apply(self, which, src, out_size):
+        """which: 0 B, 1 C, 2 vmult of the current NS stage."""
+        s = np.ascontiguousarray(src, dtype=np.float64)
+        dst = np.zeros(out_size)
+        shell_lib().orc3_apply(self.h, which, _d(dst), _d(s))
+        return dst
+
+    def set_state(self, rho, u, p):
+        r, uu, pp = (np.ascontiguousarray(a, dtype=np.float64) for a in (rho, u, p))
+        shell_lib().orc3_set_state(self.h, _d(r), _d(uu), _d(pp))
+
+    def get_state(self):
+        r, u, p = np.zeros(self.ns), np.zeros(3 * self.ns), np.zeros(self.ns)
+        shell_lib().orc3_get_state(self.h, _d(r), _d(u), _d(p))
+        return r, u, p
+
+    def run(self, n):
+        shell_lib().orc3_run(self.h, n)
+
+    def stats(self):
+        out = (ctypes.c_long * 4)()
+        shell_lib().orc3_stats(self.h, out)
+        return dict(zip(("picard_total", "gmres_total", "solve_fail", "steps"), list(out)))

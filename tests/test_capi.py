@@ -15,7 +15,7 @@ def declared():
     with open(HEADER) as fh:
         src = fh.read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(atm_[a-z0-9_]+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(atm3?_[a-z0-9_]+)\s*\(", src)))
 
 
 @pytest.fixture(scope="module")
@@ -69,7 +69,7 @@ def _prototypes():
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     out = {}
     for ret, name, args in re.findall(
-            r"^\s*((?:const\s+)?[a-z_]+\s*\**)\s*(atm_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", src,
+            r"^\s*((?:const\s+)?[a-z_]+\s*\**)\s*(atm3?_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", src,
             flags=re.M):
         params = [] if args.strip() in ("", "void") else [a.strip() for a in args.split(",")]
         # drop the parameter name, keep the type
@@ -82,6 +82,7 @@ def _ctype_of(c):
     P = ctypes.POINTER
     table = {"int": ctypes.c_int, "long": ctypes.c_long, "double": ctypes.c_double,
              "atm_handle": ctypes.c_void_p, "void*": ctypes.c_void_p,
+             "atm3_handle": ctypes.c_void_p, "atm3_handle*": P(ctypes.c_void_p),
              "constchar*": ctypes.c_char_p, "int*": P(ctypes.c_int),
              "long*": P(ctypes.c_long), "constint*": P(ctypes.c_int),
              "atm_handle*": P(ctypes.c_void_p), "void**": P(ctypes.c_void_p)}
