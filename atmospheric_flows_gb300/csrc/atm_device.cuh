@@ -42,10 +42,23 @@ constexpr int BASIS_TABLES = 8;
 static __constant__ double c_basis[KMAX + 1][BASIS_TABLES][NQ_MAX * NN_MAX];
 static __constant__ float c_basis_f[KMAX + 1][BASIS_TABLES][NQ_MAX * NN_MAX];
 
+// [degree][r][q]: the degree-2 Lagrange basis on the reference points
+// {0, 1/2, 1} at the 2k+1 Gauss points (r = 0..2 values, 3..5 derivatives)
+// and the Gauss weights (r = 6).  The FP32 Schur kernels of the multigrid
+// levels form the Jacobian of the degree-2 mapping (MeshT::map2) from it.
+constexpr int GEO2_ROWS = 7;
+static __constant__ float c_geo2_f[KMAX + 1][GEO2_ROWS][NQ_MAX];
+
+// `table` holds the basis tables ([KMAX+1][BASIS_TABLES][NQ_MAX*NN_MAX])
+// followed by the degree-2 mapping tables ([KMAX+1][GEO2_ROWS][NQ_MAX])
 static inline int upload_basis_here(const double *table) {
-  float tf[(KMAX + 1) * BASIS_TABLES * NQ_MAX * NN_MAX];
-  for (int i = 0; i < (KMAX + 1) * BASIS_TABLES * NQ_MAX * NN_MAX; ++i) tf[i] = (float)table[i];
+  constexpr int NB = (KMAX + 1) * BASIS_TABLES * NQ_MAX * NN_MAX;
+  constexpr int NG = (KMAX + 1) * GEO2_ROWS * NQ_MAX;
+  float tf[NB], tg[NG];
+  for (int i = 0; i < NB; ++i) tf[i] = (float)table[i];
+  for (int i = 0; i < NG; ++i) tg[i] = (float)table[NB + i];
   if (cudaMemcpyToSymbol(c_basis, table, sizeof(c_basis)) != cudaSuccess) return 1;
+  if (cudaMemcpyToSymbol(c_geo2_f, tg, sizeof(c_geo2_f)) != cudaSuccess) return 1;
   return cudaMemcpyToSymbol(c_basis_f, tf, sizeof(c_basis_f)) == cudaSuccess ? 0 : 1;
 }
 
@@ -506,6 +519,105 @@ __device__ __forceinline__ QGeoT<T> qgeo(const T *__restrict__ g, int q) {
   r.jxw = g[4 * NQ2 + q];
   return r;
 }
+
+// Quadrature-point geometry of cell c along the column of Gauss points
+// (g_col, g_qz), qz = 0..NQ-1, as the Schur kernels consume it.  FP64 reads
+// the stored table qgeo.  FP32 (multigrid levels) forms it from the cell's
+// degree-2 mapping (18 values instead of 5 (2k+1)^2): with
+// J = [[x_xi, x_eta], [z_xi, z_eta]] and w = w_col w_qz the entries are
+// z_eta w, -x_eta w, -z_xi w, x_xi w and det(J) w (the cofactors of J
+// times JxW / det J), contracted first along xi for the column, then along
+// eta per point.
+template <int K, typename T>
+struct GeoCol {
+  const T *G;
+  int col;
+  __device__ __forceinline__ GeoCol(const MeshT<T> &m, int c, int col_)
+      : G(m.qgeo + (long)c * 5 * (2 * K + 1) * (2 * K + 1)), col(col_) {}
+  __device__ __forceinline__ QGeoT<T> at(int qz) const {
+    return qgeo<K>(G, qz * (2 * K + 1) + col);
+  }
+  // (dxi/dx, deta/dx) JxW and (dxi/dz, deta/dz) JxW alone
+  __device__ __forceinline__ void dx(int qz, T &gxi, T &get) const {
+    constexpr int NQ2 = (2 * K + 1) * (2 * K + 1);
+    gxi = G[qz * (2 * K + 1) + col];
+    get = G[2 * NQ2 + qz * (2 * K + 1) + col];
+  }
+  __device__ __forceinline__ void dz(int qz, T &gxi, T &get) const {
+    constexpr int NQ2 = (2 * K + 1) * (2 * K + 1);
+    gxi = G[NQ2 + qz * (2 * K + 1) + col];
+    get = G[3 * NQ2 + qz * (2 * K + 1) + col];
+  }
+};
+template <int K>
+struct GeoCol<K, float> {
+  float ax[3], az[3], bx[3], bz[3], wc;  // per eta node: d/dxi and value along xi
+  __device__ __forceinline__ GeoCol(const MeshT<float> &m, int c, int col) {
+    const float2 *X = reinterpret_cast<const float2 *>(m.map2) + (long)c * 9;
+    float La[3], dLa[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      La[a] = c_geo2_f[K][a][col];
+      dLa[a] = c_geo2_f[K][3 + a][col];
+    }
+    wc = c_geo2_f[K][6][col];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      ax[e] = az[e] = bx[e] = bz[e] = 0.0f;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float2 x = __ldg(X + e * 3 + a);
+        ax[e] = fmaf(x.x, dLa[a], ax[e]);
+        az[e] = fmaf(x.y, dLa[a], az[e]);
+        bx[e] = fmaf(x.x, La[a], bx[e]);
+        bz[e] = fmaf(x.y, La[a], bz[e]);
+      }
+    }
+  }
+  __device__ __forceinline__ QGeoT<float> at(int qz) const {
+    float xxi = 0.0f, zxi = 0.0f, xet = 0.0f, zet = 0.0f;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      const float L = c_geo2_f[K][e][qz], dL = c_geo2_f[K][3 + e][qz];
+      xxi = fmaf(ax[e], L, xxi);
+      zxi = fmaf(az[e], L, zxi);
+      xet = fmaf(bx[e], dL, xet);
+      zet = fmaf(bz[e], dL, zet);
+    }
+    const float w = wc * c_geo2_f[K][6][qz];
+    QGeoT<float> r;
+    r.xx = zet * w;
+    r.xz = -xet * w;
+    r.ex = -zxi * w;
+    r.ez = xxi * w;
+    r.jxw = (xxi * zet - xet * zxi) * w;
+    return r;
+  }
+  // (dxi/dx, deta/dx) JxW = (z_eta, -z_xi) w: the z coordinate alone
+  __device__ __forceinline__ void dx(int qz, float &gxi, float &get) const {
+    float zxi = 0.0f, zet = 0.0f;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      zxi = fmaf(az[e], c_geo2_f[K][e][qz], zxi);
+      zet = fmaf(bz[e], c_geo2_f[K][3 + e][qz], zet);
+    }
+    const float w = wc * c_geo2_f[K][6][qz];
+    gxi = zet * w;
+    get = -zxi * w;
+  }
+  // (dxi/dz, deta/dz) JxW = (-x_eta, x_xi) w: the x coordinate alone
+  __device__ __forceinline__ void dz(int qz, float &gxi, float &get) const {
+    float xxi = 0.0f, xet = 0.0f;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      xxi = fmaf(ax[e], c_geo2_f[K][e][qz], xxi);
+      xet = fmaf(bx[e], c_geo2_f[K][3 + e][qz], xet);
+    }
+    const float w = wc * c_geo2_f[K][6][qz];
+    gxi = -xet * w;
+    get = xxi * w;
+  }
+};
 
 // tiles, x-contraction exchange, face values [, subface-1 face values]
 template <int K, typename T = double>

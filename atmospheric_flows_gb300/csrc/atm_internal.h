@@ -82,6 +82,12 @@ struct MeshT {
   // every dt-weighted term (stage fluxes, gravity, B, C, sponge) uses the
   // member's own step; members share no faces, so a row scale is exact.
   T *dts = nullptr;
+  // [nc][3][3][2] the mapping at degree 2: (x, z) at the reference points
+  // (xi, eta) in {0, 1/2, 1}^2, eta slowest.  Exact for mapping degree <= 2,
+  // its interpolant otherwise.  The FP32 multigrid levels form their
+  // quadrature-point geometry from it in the Schur kernels instead of
+  // reading qgeo (null on the FP64 operator mesh).
+  T *map2 = nullptr;
 };
 using Mesh = MeshT<double>;
 
@@ -121,6 +127,9 @@ struct atm_ctx {
   // device address of the static Schur scratch array in this handle's
   // context (atm_schur_vmult_static_scratch; looked up on first use)
   void *static_scratch = nullptr;
+  // host copy of the operator mesh's mapping at degree 2 (MeshT::map2
+  // layout): the geometry of the FP32 multigrid level 0
+  std::vector<double> map2;
   long n_scalar() const { return (long)nc * nn2; }
   long n_vector() const { return 2L * nc * nn2; }
 };
@@ -296,6 +305,7 @@ struct HostMesh {
   std::vector<int> nbr, nbrf;
   std::vector<int> hnb;      // [nhang][2]
   std::vector<double> hgeo;  // [nhang][2][3][nq]
+  std::vector<double> map2;  // [nc][3][3][2] the mapping at degree 2 (MeshT::map2)
   int nhang = 0;
 };
 int build_mesh_tables(int k, int nc, int mapdeg, const double *nodes, int n_inner,

@@ -282,7 +282,7 @@ MGHier<double> &hier<double>(MG &mg) { return mg.d; }
 template <typename T>
 void level_free(MGLevelT<T> &L) {
   cudaFree(L.mesh.qgeo); cudaFree(L.mesh.fgeo); cudaFree(L.mesh.nbr); cudaFree(L.mesh.nbrf);
-  cudaFree(L.mesh.hnb); cudaFree(L.mesh.hgeo); cudaFree(L.mesh.dts);
+  cudaFree(L.mesh.hnb); cudaFree(L.mesh.hgeo); cudaFree(L.mesh.dts); cudaFree(L.mesh.map2);
   cudaFree(L.parent); cudaFree(L.ppos); cudaFree(L.children);
   cudaFree(L.ainv); cudaFree(L.invd); cudaFree(L.rho); cudaFree(L.pfix);
   cudaFree(L.pfq); cudaFree(L.pff);
@@ -334,6 +334,16 @@ int level_alloc(atm_ctx &c, MGLevelT<T> &L, const HostMesh &hm) {
   L.mesh.nc = L.nc; L.mesh.k = c.k; L.mesh.nn = c.nn; L.mesh.nq = nq;
   L.mesh.nn2 = nn2; L.mesh.nq2 = nq2;
   std::vector<T> qf(hm.qgeo.begin(), hm.qgeo.end()), ff(hm.fgeo.begin(), hm.fgeo.end());
+  if (hm.map2.size() != (size_t)L.nc * 18) {
+    set_error("multigrid level: missing degree-2 mapping table");
+    return ATM_BAD_ARG;
+  }
+  if (sizeof(T) == 4) {  // the FP32 Schur kernels form their geometry from it
+    std::vector<T> m2(hm.map2.begin(), hm.map2.end());
+    ATM_CUDA(cudaMalloc(&L.mesh.map2, m2.size() * sizeof(T)));
+    ATM_CUDA(cudaMemcpyAsync(L.mesh.map2, m2.data(), m2.size() * sizeof(T), cudaMemcpyHostToDevice, c.stream));
+    ATM_CUDA(cudaStreamSynchronize(c.stream));  // pageable source
+  }
   ATM_CUDA(cudaMalloc(&L.mesh.qgeo, qf.size() * sizeof(T)));
   ATM_CUDA(cudaMalloc(&L.mesh.fgeo, ff.size() * sizeof(T)));
   ATM_CUDA(cudaMalloc(&L.mesh.nbr, hm.nbr.size() * sizeof(int)));
@@ -728,6 +738,7 @@ int mg_add_level(atm_ctx &c, int n_cells, int mapdeg, const double *nodes, int n
     hm.nhang = c.mesh.nhang;
     hm.hnb.resize((size_t)c.mesh.nhang * 2);
     hm.hgeo.resize((size_t)c.mesh.nhang * 2 * 3 * c.nq);
+    hm.map2 = c.map2;
     ATM_CUDA(cudaMemcpyAsync(hm.qgeo.data(), c.mesh.qgeo, hm.qgeo.size() * 8, cudaMemcpyDeviceToHost, c.stream));
     ATM_CUDA(cudaMemcpyAsync(hm.fgeo.data(), c.mesh.fgeo, hm.fgeo.size() * 8, cudaMemcpyDeviceToHost, c.stream));
     ATM_CUDA(cudaMemcpyAsync(hm.nbr.data(), c.mesh.nbr, hm.nbr.size() * 4, cudaMemcpyDeviceToHost, c.stream));

@@ -42,17 +42,19 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     const T *tl = tiles + lc * NT * NN2;
     T pv[NQ];
     eval_col<K>(tl, Sx, pv);
-    const T *G = mesh.qgeo + (long)c * 5 * NQ2;
+    const GeoCol<K, T> G(mesh, c, col);
     T V[NQ], Gxi[NQ], Get[NQ];
     // submit_divergence(-cB p): component d is tested with d(phi)/dx_d
 #pragma unroll
     for (int comp = 0; comp < 2; ++comp) {
 #pragma unroll
       for (int qz = 0; qz < NQ; ++qz) {
-        const auto g = qgeo<K>(G, qz * NQ + col);
+        T gxi, get;
+        if (comp == 0) G.dx(qz, gxi, get);
+        else G.dz(qz, gxi, get);
         const T s = -cB * pv[qz];
-        Gxi[qz] = (comp == 0 ? g.xx : g.xz) * s;
-        Get[qz] = (comp == 0 ? g.ex : g.ez) * s;
+        Gxi[qz] = gxi * s;
+        Get[qz] = get * s;
         V[qz] = T(0.0);
       }
       T *xa = xab + (lc * 2 + comp) * 2 * NN * NQ;
@@ -147,8 +149,9 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
   // points (pfq) and its face traces (pff), prepared when p_fix is set.  The
   // hanging-face variant reads the p_fix tile (its traces are needed at
   // subface points): w(2), pfix, [p].
-  constexpr int NT = (HG ? 3 : 2) + (WITH_D ? 1 : 0);
-  constexpr int TP = HG ? 3 : 2;  // tile of p
+  constexpr bool PT = HG;  // p_fix tile
+  constexpr int NT = (PT ? 3 : 2) + (WITH_D ? 1 : 0);
+  constexpr int TP = PT ? 3 : 2;  // tile of p
   constexpr T GM1 = GAS_GAMMA - T(1.0);
   constexpr T HG_ = GAS_GAMMA / (GAS_GAMMA - T(1.0));  // enthalpy factor
   // sign of the C contribution in dst
@@ -163,7 +166,7 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
   const int c0 = blockIdx.x * CPB;
   const int cnt = min(CPB, mesh.nc - c0);
   load_tiles<K>(tiles, NT, 0, w, 2, c0, cnt);
-  if (HG) load_tiles<K>(tiles, NT, 2, pfix, 1, c0, cnt);
+  if (PT) load_tiles<K>(tiles, NT, 2, pfix, 1, c0, cnt);
   if (WITH_D) load_tiles<K>(tiles, NT, TP, p, 1, c0, cnt);
   __syncthreads();
   const bool active = lc < cnt;
@@ -176,18 +179,18 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     T wx[NQ], wz[NQ], pf[NQ], pv[NQ];
     eval_col<K>(tl, Sx, wx);
     eval_col<K>(tl + NN2, Sx, wz);
-    if (HG) {
+    if (PT) {
       eval_col<K>(tl + 2 * NN2, Sx, pf);
     } else {
 #pragma unroll
       for (int qz = 0; qz < NQ; ++qz) pf[qz] = pfq[(long)c * NQ2 + qz * NQ + col];
     }
     if (WITH_D) eval_col<K>(tl + TP * NN2, Sx, pv);
-    const T *G = mesh.qgeo + (long)c * 5 * NQ2;
+    const GeoCol<K, T> G(mesh, c, col);
     T V[NQ], Gxi[NQ], Get[NQ];
 #pragma unroll
     for (int qz = 0; qz < NQ; ++qz) {
-      const auto g = qgeo<K>(G, qz * NQ + col);
+      const auto g = G.at(qz);
       // C: submit_gradient(-cC hg pfix w)
       const T gx = SC * (-cC * HG_ * pf[qz] * wx[qz]);
       const T gz = SC * (-cC * HG_ * pf[qz] * wz[qz]);

@@ -116,7 +116,12 @@ int upload_basis_all() {
   // [k][w][q*(k+1)+i]: w = 0 values, 1 derivatives at the Gauss points,
   // 2 and 3 values at the subface points (g_q + s)/2 (hanging faces)
   constexpr int NW = 8;
-  std::vector<double> tab((KMAX + 1) * NW * NQ_MAX * NN_MAX, 0.0);
+  static_assert(NW == BASIS_TABLES, "basis table count");
+  // followed by the degree-2 mapping tables [k][r][q] (r = 0..2 values and
+  // 3..5 derivatives of the Lagrange basis on {0, 1/2, 1}, 6 Gauss weights)
+  constexpr size_t NB = (size_t)(KMAX + 1) * NW * NQ_MAX * NN_MAX;
+  std::vector<double> tab(NB + (size_t)(KMAX + 1) * GEO2_ROWS * NQ_MAX, 0.0);
+  const std::vector<double> m2 = gll_nodes(2);
   for (int k = 1; k <= KMAX; ++k) {
     HostBasis b = make_basis(k);
     double *S = &tab[(k * NW + 0) * NQ_MAX * NN_MAX];
@@ -127,6 +132,15 @@ int upload_basis_all() {
       double *H = &tab[(k * NW + 2 + s) * NQ_MAX * NN_MAX];
       for (int q = 0; q < b.nq; ++q)
         lagrange_eval(b.gll, 0.5 * (b.gauss[q] + s), &H[q * b.nn], nullptr);
+    }
+    for (int q = 0; q < b.nq; ++q) {
+      double v[3], d[3];
+      lagrange_eval(m2, b.gauss[q], v, d);
+      for (int a = 0; a < 3; ++a) {
+        tab[NB + ((size_t)k * GEO2_ROWS + a) * NQ_MAX + q] = v[a];
+        tab[NB + ((size_t)k * GEO2_ROWS + 3 + a) * NQ_MAX + q] = d[a];
+      }
+      tab[NB + ((size_t)k * GEO2_ROWS + 6) * NQ_MAX + q] = b.weights[q];
     }
     // even/odd halves for q < k, i < (k+1)/2 (same [q*(k+1)+i] indexing)
     for (int w = 0; w < 2; ++w) {
@@ -335,6 +349,24 @@ int build_mesh_tables(int k, int nc, int mapdeg, const double *nodes, int n_inne
         face_geo(cell, f, Lg[q].data(), dLg[q].data(), b.weights[q], &fgeo[base + q], nq);
       }
   }
+  // the mapping at degree 2: its values at (xi, eta) in {0, 1/2, 1}^2
+  out.map2.assign((size_t)nc * 18, 0.0);
+  {
+    std::vector<double> L2[3];
+    for (int a = 0; a < 3; ++a) {
+      L2[a].resize(mn);
+      lagrange_eval(mx, 0.5 * a, L2[a].data(), nullptr);
+    }
+    for (int cell = 0; cell < nc; ++cell)
+      for (int e = 0; e < 3; ++e)
+        for (int a = 0; a < 3; ++a)
+          for (int bb = 0; bb < mn; ++bb)
+            for (int aa = 0; aa < mn; ++aa) {
+              const double *X = nodes + (((size_t)cell * mn + bb) * mn + aa) * 2;
+              const double w = L2[a][aa] * L2[e][bb];
+              for (int d = 0; d < 2; ++d) out.map2[(size_t)cell * 18 + (e * 3 + a) * 2 + d] += w * X[d];
+            }
+  }
   // subface geometry of the coarse side of every hanging face, at the points
   // (g_q + s)/2 of the coarse face with weights w_q/2
   out.hgeo.assign((size_t)out.nhang * 2 * 3 * nq, 0.0);
@@ -378,6 +410,7 @@ int mesh_upload(atm_ctx &c, int mapdeg, const double *nodes, int n_inner, const 
   }
   m.nhang = hm.nhang;
   c.mapdeg = mapdeg;
+  c.map2 = std::move(hm.map2);
   rc = launch_block_inverse(c, m.minv, nullptr);
   if (rc) return rc;
   rc = launch_inv_diag(c, c.invdiag_D, 1, nullptr, 1.0 / (GAS_GAMMA - 1.0));

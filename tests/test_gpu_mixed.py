@@ -65,6 +65,26 @@ def test_vcycle_reduces_residual(cuda_ok, k, precision):
     assert red < 0.5, red
 
 
+@pytest.mark.parametrize("mapping_degree,bar", [(1, 1e-4), (2, 1e-4), (3, 1e-2)])
+def test_fp32_vcycle_follows_the_fp64_vcycle(cuda_ok, mapping_degree, bar):
+    """The FP32 levels form their quadrature geometry from the degree-2
+    mapping: the FP32 V-cycle equals the FP64 one to FP32 round-off when the
+    mapping degree is at most 2; at degree 3 the FP32 levels see the
+    mapping's degree-2 interpolant, a small change of the preconditioner."""
+    case = build_case(HillParams(nx=32, nz=16, degree=4, cfl=5.0,
+                                 mapping_degree=mapping_degree))
+    op, rng = schur_op(case)
+    b = dev(rng.standard_normal(op.n_scalar))
+    z1, z2 = torch.empty_like(b), torch.empty_like(b)
+    op.mg_vcycle(z1, b, 1)
+    op.mg_vcycle(z2, b, 2)
+    d = ((z1 - z2).norm() / z2.norm()).item()
+    assert d < bar, d
+    r = torch.empty_like(b)
+    op.vmult(r, z1)
+    assert ((b - r).norm() / b.norm()).item() < 0.5
+
+
 def test_fgmres_beats_jacobi_gmres(cuda_ok):
     case = build_case(HillParams(nx=32, nz=16, degree=4, cfl=5.0))
     op, rng = schur_op(case)
