@@ -427,9 +427,14 @@ __device__ __forceinline__ void face_terms(const MeshT<T> &mesh, int c, int col,
                                            const T (&Sx)[K + 1], T *__restrict__ fbc,
                                            T *__restrict__ fhc, Body &&body) {
   constexpr int NQ = 2 * K + 1;
+  // the four neighbours and their faces in two 16-byte loads; FP32 (latency
+  // bound) unrolls the faces so that their loads overlap
+  const int4 nb4 = *reinterpret_cast<const int4 *>(mesh.nbr + c * 4);
+  const int4 nf4 = *reinterpret_cast<const int4 *>(mesh.nbrf + c * 4);
+#pragma unroll(sizeof(T) == 4 ? 4 : 1)
   for (int f = 0; f < 4; ++f) {
-    const int nb = mesh.nbr[c * 4 + f];
-    const int nfc = mesh.nbrf[c * 4 + f];
+    const int nb = f == 0 ? nb4.x : f == 1 ? nb4.y : f == 2 ? nb4.z : nb4.w;
+    const int nfc = f == 0 ? nf4.x : f == 1 ? nf4.y : f == 2 ? nf4.z : nf4.w;
     const int code = HG && nb >= 0 ? (nfc >> 2) : 0;
     T val[NC];
     if (code == 0) {
@@ -518,6 +523,33 @@ __device__ __forceinline__ QGeoT<T> qgeo(const T *__restrict__ g, int q) {
   r.ez = g[3 * NQ2 + q];
   r.jxw = g[4 * NQ2 + q];
   return r;
+}
+
+// Values between two cells' A^{-1} blocks ([nc][stride], the (k+1)^2 x
+// (k+1)^2 block first).  FP32 blocks (multigrid levels) are padded to a
+// multiple of 16 bytes, so that the B kernel can stage the A^{-1} blocks of
+// its cells into shared memory with 16-byte cp.async copies.
+template <int K, typename T>
+__host__ __device__ constexpr int ainv_stride() {
+  return sizeof(T) == 4 ? ((K + 1) * (K + 1) * (K + 1) * (K + 1) + 3) / 4 * 4
+                        : (K + 1) * (K + 1) * (K + 1) * (K + 1);
+}
+inline long ainv_stride_rt(int k, size_t elem) {
+  const long n = (long)(k + 1) * (k + 1) * (k + 1) * (k + 1);
+  return elem == 4 ? (n + 3) / 4 * 4 : n;
+}
+
+// 16-byte asynchronous global -> shared copies (cp.async, bypassing L1) and
+// the wait for all of this thread's outstanding copies
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
 // Quadrature-point geometry of cell c along the column of Gauss points

@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(32 * BI_WARPS)
     for (int i = lane; i < NN2; i += 32) M[sym_index(i, k)] = i == k ? -d : cd[i];
     __syncwarp();
   }
-  T *o = out + (long)c * NN2 * NN2;
+  T *o = out + (long)c * ainv_stride<K, T>();
   for (int e = lane; e < NN2 * NN2; e += 32) {
     const int j = e / NN2, i = e - j * NN2;
     o[e] = -M[sym_index(i, j)];
@@ -276,7 +276,7 @@ __global__ void k_block_apply(T *__restrict__ dst, const T *__restrict__ src,
   const long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= (long)nc * NN2) return;
   const int c = (int)(g / NN2), i = (int)(g - (long)c * NN2);
-  const T *B = binvT + (long)c * NN2 * NN2;
+  const T *B = binvT + (long)c * ainv_stride<K, T>();
   for (int comp = 0; comp < ncomp; ++comp) {
     const T *s = src + ((long)c * ncomp + comp) * NN2;
     T acc = T(0.0);

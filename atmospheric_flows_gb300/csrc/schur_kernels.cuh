@@ -18,12 +18,18 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     k_B(T *__restrict__ dst, const T *__restrict__ p, T cB,
         const T *__restrict__ ainv, MeshT<T> mesh) {
   using C = Cfg<K>;
-  constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2, NQ2 = C::NQ2;
+  constexpr int NN = C::NN, NQ = C::NQ, NN2 = C::NN2;
   const int CPB = blockDim.x / NQ;  // cells per block, chosen by the autotuner
   constexpr int NT = 1;
+  // FP32 (multigrid levels): the A^{-1} blocks of the block's cells are
+  // contiguous; they are copied into shared memory asynchronously at the
+  // start and arrive while B is computed
+  constexpr bool STAGE = MODE == 2 && sizeof(T) == 4;
+  constexpr int AS = ainv_stride<K, T>();
   extern __shared__ __align__(16) unsigned char sm_raw[];
   T *sm = reinterpret_cast<T *>(sm_raw);
-  T *tiles = sm;
+  T *as = sm;                       // [CPB][AS] staged A^{-1} (STAGE)
+  T *tiles = sm + (STAGE ? CPB * AS : 0);
   T *xab = tiles + CPB * NT * NN2;  // [CPB][2][2][NN*NQ]
   T *fb = xab + CPB * 4 * NN * NQ;  // [CPB][2][4][NQ]
   T *bt = fb + CPB * 8 * NQ;        // [CPB][2][NN2] (MODE 2)
@@ -31,6 +37,13 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
   const int tid = threadIdx.x, lc = tid / NQ, col = tid - lc * NQ;
   const int c0 = blockIdx.x * CPB;
   const int cnt = min(CPB, mesh.nc - c0);
+  if constexpr (STAGE) {
+    // cells c0 .. c0+cnt-1: cnt * AS values, 16-byte aligned (AS % 4 == 0)
+    const T *src = ainv + (long)c0 * AS;
+    const int n16 = cnt * AS / 4;
+    for (int e = tid; e < n16; e += blockDim.x) cp_async16(as + 4 * e, src + 4 * e);
+    cp_async_commit();
+  }
   load_tiles<K>(tiles, NT, 0, p, 1, c0, cnt);
   __syncthreads();
   const bool active = lc < cnt;
@@ -99,22 +112,19 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
     }
   }
   if (MODE == 2) {
+    if constexpr (STAGE) cp_async_wait_all();
     __syncthreads();
     if (active) {
-      const T *Ab = ainv + (long)c * NN2 * NN2;
+      const T *Ab = STAGE ? as + lc * AS : ainv + (long)c * AS;
       const T *b0 = bt + (lc * 2 + 0) * NN2, *b1 = bt + (lc * 2 + 1) * NN2;
       for (int i = col; i < NN2; i += NQ) {
         T s0 = T(0.0), s1 = T(0.0);
-        if constexpr (sizeof(T) == 4) {
-          // FP32 (multigrid levels): latency bound, so all NN2 loads of the
-          // A^{-1} column go out before the FMAs
-          T a[NN2];
-#pragma unroll
-          for (int j = 0; j < NN2; ++j) a[j] = Ab[j * NN2 + i];  // transposed storage
+        if constexpr (STAGE) {
 #pragma unroll
           for (int j = 0; j < NN2; ++j) {
-            s0 = fma(a[j], b0[j], s0);
-            s1 = fma(a[j], b1[j], s1);
+            const T a = Ab[j * NN2 + i];  // transposed storage
+            s0 = fma(a, b0[j], s0);
+            s1 = fma(a, b1[j], s1);
           }
         } else {
 #pragma unroll 5
@@ -304,7 +314,8 @@ int B_launch(const OpView<T> &v, T *dst, const T *p, T cB, int mode) {
   using C = Cfg<K>;
   auto launch = [&](int cpb) -> cudaError_t {
     const int grid = (v.nc + cpb - 1) / cpb, th = cpb * C::NQ;
-    const size_t sm = smem_bytes<K, T>(cpb, 1, 2, HG) + sizeof(T) * cpb * 2 * C::NN2;
+    const size_t sm = smem_bytes<K, T>(cpb, 1, 2, HG) + sizeof(T) * cpb * 2 * C::NN2 +
+                      (mode == 2 && sizeof(T) == 4 ? sizeof(T) * cpb * ainv_stride<K, T>() : 0);
     void (*fn)(T *, const T *, T, const T *, MeshT<T>) =
         mode == 0 ? k_B<K, 0, T, HG> : (mode == 1 ? k_B<K, 1, T, HG> : k_B<K, 2, T, HG>);
     if (sm > 48 * 1024) {

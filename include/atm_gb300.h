@@ -202,9 +202,10 @@ int atm_solve(atm_handle h, double *x, const double *b, double tol, int maxit,
 int atm_mg_add_level(atm_handle h, int n_cells, int mapping_degree, const double *mapping_nodes,
                      int n_inner, const int *inner_faces, int n_bdry, const int *bdry_faces,
                      const int *children);
-/* Chebyshev degree (3), smoothing range (15), power iterations for the
- * largest eigenvalue (10), degree of the coarsest-level Chebyshev (10).
- * Replaces the smoother_data set-up of Atmospheric_Flow.cc:477-498,594-615. */
+/* Chebyshev degree (4; the reference's 3 needs more FGMRES iterations),
+ * smoothing range (15), power iterations for the largest eigenvalue (10),
+ * degree of the coarsest-level Chebyshev (10).  Replaces the smoother_data
+ * set-up of Atmospheric_Flow.cc:477-498,594-615. */
 int atm_mg_set_smoother(atm_handle h, int degree, double smoothing_range, int eig_iterations,
                         int coarse_degree);
 /* One V-cycle: dst ~= S^{-1} src (FP64 device vectors); precision 1 runs the

@@ -1,7 +1,11 @@
 """The 3D shell path on the GB300 against the 3D oracle: every operator at
-1e-12, IMEX steps at 1e-10 (tight solves on both sides), and the reference's
-known answer (the exact steady solid-body rotation) on the reference's cell
-count, 6144 cells."""
+1e-12, IMEX steps at 1e-10 (tight solves on both sides), and, on the
+reference's cell count (6144 cells), the errors against the reference's known
+answer (the exact steady solid-body rotation) step by step as the oracle
+gives them."""
+import json
+import os
+
 import numpy as np
 import pytest
 
@@ -103,24 +107,35 @@ def test_steps_match_oracle(cuda_ok, rotated):
     g.close()
 
 
-def test_reference_cell_count_keeps_the_steady_state(cuda_ok):
-    """6144 cells (the reference's concentric_hyper_shells refined 3 times
-    has as many), thin shell, 20 steps of 8.64 s: density and pressure stay
-    at their interpolation error, the wind error stays below 5%."""
-    case = build_shell(ShellParams(n=16, nr=4, r_in=EARTH_A, r_out=EARTH_A + 1.0e4))
-    assert case.n_cells == 6144
-    g = ShellSolver(case, eps=1e-12, scaled_tol=True, true_residual_check=True)
+FIXTURE = os.path.join(os.path.dirname(__file__), "golden", "oracle_shell_6144_errors.json")
+
+
+def test_reference_cell_count_follows_the_oracle(cuda_ok):
+    """6144 cells (the reference's concentric_hyper_shells refined three
+    times has as many), thin shell, 20 steps of 8.64 s.  At every step the
+    errors against the exact steady state (what the reference's
+    analyze_results prints) equal the oracle's to 1e-6 relative (fixture:
+    tests/golden/make_shell_errors.py).  Those errors grow from the
+    interpolation level: the Q1 shell's discrete balance is not the exact
+    one, and the drift shrinks under refinement (tests/test_shell.py)."""
+    with open(FIXTURE) as fh:
+        ref = json.load(fh)
+    cfg = ref["config"]
+    case = build_shell(ShellParams(n=cfg["n"], nr=cfg["nr"], r_in=EARTH_A,
+                                   r_out=EARTH_A + cfg["thickness"]))
+    assert case.n_cells == ref["n_cells"] == 6144
+    g = ShellSolver(case, eps=cfg["eps"], scaled_tol=True, true_residual_check=True)
 
     def errs(state):
         r, u, p = state
         return exact_l2_errors(case, {"rho": nodal_to_quad(case, r),
                                       "u": nodal_to_quad(case, u, 3), "p": nodal_to_quad(case, p)})
 
-    e0 = errs(g.get_state())
-    g.run(20)
-    e = errs(g.get_state())
+    for step, want in enumerate(ref["errors"]):
+        if step:
+            g.run(1)
+        got = errs(g.get_state())
+        for f in ("rho", "u", "p"):
+            assert abs(got[f] - want[f]) <= 1e-6 * want[f], (step, f, got[f], want[f])
     assert g.stats()["solve_fail"] == 0
-    for f in ("rho", "p"):
-        assert e[f] < 1.2 * e0[f], (f, e0[f], e[f])
-    assert e["u"] < 0.05, e
     g.close()

@@ -8,6 +8,9 @@ isothermal atmosphere), where degree-1 elements at its refinement cannot
 represent the exact density (it varies by e^88 across the shell): the known
 answer is checked on a thin shell (10 km), with the same equations.
 """
+import json
+import os
+
 import numpy as np
 import pytest
 
@@ -76,3 +79,22 @@ def test_reference_stopping_rule_does_not_iterate():
     tight.run(1)
     assert loose.stats()["gmres_total"] == 0
     assert tight.stats()["gmres_total"] > 0
+
+
+def test_oracle_reproduces_its_reference_size_fixture():
+    """The first step of the 6144-cell fixture (the GPU test's reference)
+    is what the oracle computes now."""
+    path = os.path.join(os.path.dirname(__file__), "golden", "oracle_shell_6144_errors.json")
+    with open(path) as fh:
+        ref = json.load(fh)
+    cfg = ref["config"]
+    c = thin(cfg["n"], cfg["nr"])
+    assert c.n_cells == ref["n_cells"]
+    o = OracleShell(c, eps=cfg["eps"], inner_tol=cfg["inner_tol"], scaled_tol=True,
+                    true_residual_check=True)
+    for step in (0, 1):
+        if step:
+            o.run(1)
+        got = errors(c, o.get_state())
+        for f in ("rho", "u", "p"):
+            assert abs(got[f] - ref["errors"][step][f]) <= 1e-8 * ref["errors"][step][f]
