@@ -525,18 +525,21 @@ __device__ __forceinline__ QGeoT<T> qgeo(const T *__restrict__ g, int q) {
   return r;
 }
 
-// Values between two cells' A^{-1} blocks ([nc][stride], the (k+1)^2 x
-// (k+1)^2 block first).  FP32 blocks (multigrid levels) are padded to a
-// multiple of 16 bytes, so that the B kernel can stage the A^{-1} blocks of
-// its cells into shared memory with 16-byte cp.async copies.
+// Values between two cells' A^{-1} blocks ([nc][stride]).  FP64: the full
+// (k+1)^2 x (k+1)^2 block.  FP32 (multigrid levels): A^{-1} is symmetric, so
+// only its lower triangle is stored, row by row ((r, c <= r) at
+// r (r+1)/2 + c), padded to a multiple of 16 bytes: the B kernel stages the
+// blocks of its cells into shared memory with 16-byte cp.async copies, and
+// half the bytes leave more room there.
 template <int K, typename T>
 __host__ __device__ constexpr int ainv_stride() {
-  return sizeof(T) == 4 ? ((K + 1) * (K + 1) * (K + 1) * (K + 1) + 3) / 4 * 4
-                        : (K + 1) * (K + 1) * (K + 1) * (K + 1);
+  return sizeof(T) == 4
+             ? ((K + 1) * (K + 1) * ((K + 1) * (K + 1) + 1) / 2 + 3) / 4 * 4
+             : (K + 1) * (K + 1) * (K + 1) * (K + 1);
 }
 inline long ainv_stride_rt(int k, size_t elem) {
-  const long n = (long)(k + 1) * (k + 1) * (k + 1) * (k + 1);
-  return elem == 4 ? (n + 3) / 4 * 4 : n;
+  const long n2 = (long)(k + 1) * (k + 1);
+  return elem == 4 ? (n2 * (n2 + 1) / 2 + 3) / 4 * 4 : n2 * n2;
 }
 
 // 16-byte asynchronous global -> shared copies (cp.async, bypassing L1) and

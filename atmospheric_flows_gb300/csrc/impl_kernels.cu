@@ -261,9 +261,13 @@ __global__ void __launch_bounds__(32 * BI_WARPS)
     __syncwarp();
   }
   T *o = out + (long)c * ainv_stride<K, T>();
-  for (int e = lane; e < NN2 * NN2; e += 32) {
-    const int j = e / NN2, i = e - j * NN2;
-    o[e] = -M[sym_index(i, j)];
+  if constexpr (sizeof(T) == 4) {  // packed lower triangle (ainv_stride)
+    for (int e = lane; e < NTRI; e += 32) o[e] = -M[e];
+  } else {
+    for (int e = lane; e < NN2 * NN2; e += 32) {
+      const int j = e / NN2, i = e - j * NN2;
+      o[e] = -M[sym_index(i, j)];
+    }
   }
 }
 
@@ -273,6 +277,7 @@ __global__ void k_block_apply(T *__restrict__ dst, const T *__restrict__ src,
                               const T *__restrict__ binvT, int ncomp, T scale,
                               int nc) {
   constexpr int NN2 = (K + 1) * (K + 1);
+  static_assert(sizeof(T) == 8, "full A^{-1} blocks are FP64 (FP32 stores a triangle)");
   const long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= (long)nc * NN2) return;
   const int c = (int)(g / NN2), i = (int)(g - (long)c * NN2);

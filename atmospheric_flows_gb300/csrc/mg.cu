@@ -372,6 +372,9 @@ int level_alloc(atm_ctx &c, MGLevelT<T> &L, const HostMesh &hm) {
   }
   ATM_CUDA(cudaMalloc(&L.wv, 2 * ns * sizeof(T)));
   ATM_CUDA(cudaMalloc(&L.ainv, (size_t)L.nc * ainv_stride_rt(c.k, sizeof(T)) * sizeof(T)));
+  // the padding after each FP32 triangle is copied but never used
+  ATM_CUDA(cudaMemsetAsync(L.ainv, 0, (size_t)L.nc * ainv_stride_rt(c.k, sizeof(T)) * sizeof(T),
+                           c.stream));
   ATM_CUDA(cudaMalloc(&L.pfq, (size_t)L.nc * c.nq2 * sizeof(T)));
   ATM_CUDA(cudaMalloc(&L.pff, (size_t)L.nc * 4 * c.nq * sizeof(T)));
   return level_inv_diag<T>(lview(c, L), L.invd, (T)(1.0 / (GAS_GAMMA - 1.0)));
@@ -443,10 +446,10 @@ int level_apply(atm_ctx &c, MGLevelT<T> &L, T *out, const T *x) {
   const double co = implicit_coeff(c);
   LevelViewT<T> v = lview(c, L);
   // algorithmic bytes: x, pfix, invd-free D/C read + B/A^{-1} intermediate
-  // (2 comps written + read) + A^{-1} + out; flops: the FP64 formulas of
+  // (2 comps written + read) + A^{-1} as stored (FP32: its triangle) + out; flops: the FP64 formulas of
   // launch_B (mode 2) and launch_CD (mode 1)
   const double ns = (double)L.nc * c.nn2, sz = sizeof(T);
-  const double bytes = sz * (ns * (1 + 2 + 2 + 1 + 1 + 1) + (double)L.nc * c.nn2 * c.nn2);
+  const double bytes = sz * (ns * (1 + 2 + 2 + 1 + 1 + 1) + (double)L.nc * ainv_stride_rt(c.k, sz));
   const double flops = L.nc * (fl_eval(c.k) + 2 * fl_integrate(c.k, true) + 4.0 * 4 * fl_face(c.k) +
                                4.0 * c.nn2 * c.nn2 + 4 * fl_eval(c.k) + fl_integrate(c.k, true) +
                                4.0 * 7 * fl_face(c.k));
@@ -465,7 +468,7 @@ int level_apply_cheb(atm_ctx &c, MGLevelT<T> &L, double a, double b_coef, bool f
   LevelViewT<T> v = lview(c, L);
   const double ns = (double)L.nc * c.nn2, sz = sizeof(T);
   // as level_apply, plus rhs, invd, d read and d, x written in the update
-  const double bytes = sz * (ns * (1 + 2 + 2 + 1 + 1 + 5) + (double)L.nc * c.nn2 * c.nn2);
+  const double bytes = sz * (ns * (1 + 2 + 2 + 1 + 1 + 5) + (double)L.nc * ainv_stride_rt(c.k, sz));
   const double flops = L.nc * (fl_eval(c.k) + 2 * fl_integrate(c.k, true) + 4.0 * 4 * fl_face(c.k) +
                                4.0 * c.nn2 * c.nn2 + 4 * fl_eval(c.k) + fl_integrate(c.k, true) +
                                4.0 * 7 * fl_face(c.k));

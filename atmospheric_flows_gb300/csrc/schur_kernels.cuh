@@ -120,9 +120,12 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
       for (int i = col; i < NN2; i += NQ) {
         T s0 = T(0.0), s1 = T(0.0);
         if constexpr (STAGE) {
+          // packed lower triangle: A_ij at i(i+1)/2 + j (j <= i), else
+          // j(j+1)/2 + i; the same values in the same order as the full block
+          const int ri = i * (i + 1) / 2;
 #pragma unroll
           for (int j = 0; j < NN2; ++j) {
-            const T a = Ab[j * NN2 + i];  // transposed storage
+            const T a = j <= i ? Ab[ri + j] : Ab[j * (j + 1) / 2 + i];
             s0 = fma(a, b0[j], s0);
             s1 = fma(a, b1[j], s1);
           }
@@ -147,7 +150,7 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
 // MODE 4: t = sD D p - C w with p = ch.x, then the Chebyshev update of ch
 //         (x and d, with rhs and invd) instead of a store of t
 template <int K, int MODE, typename T, bool HG>
-__global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
+__global__ void __launch_bounds__(Cfg<K>::MAX_THREADS, sizeof(T) == 4 ? 4 : 1)
     k_CD(T *__restrict__ dst, const T *__restrict__ w, const T *__restrict__ p,
          const T *__restrict__ pfix, const T *__restrict__ pfq, const T *__restrict__ pff,
          T cC, const T *__restrict__ invd, MeshT<T> mesh, ChebArgs<T> ch) {

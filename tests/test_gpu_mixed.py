@@ -65,13 +65,16 @@ def test_vcycle_reduces_residual(cuda_ok, k, precision):
     assert red < 0.5, red
 
 
-@pytest.mark.parametrize("mapping_degree,bar", [(1, 1e-4), (2, 1e-4), (3, 1e-2)])
-def test_fp32_vcycle_follows_the_fp64_vcycle(cuda_ok, mapping_degree, bar):
+@pytest.mark.parametrize("degree,mapping_degree,bar",
+                         [(4, 1, 1e-4), (4, 2, 1e-4), (4, 3, 1e-2), (1, 2, 1e-4), (3, 2, 1e-4),
+                          (5, 2, 1e-4)])
+def test_fp32_vcycle_follows_the_fp64_vcycle(cuda_ok, degree, mapping_degree, bar):
     """The FP32 levels form their quadrature geometry from the degree-2
-    mapping: the FP32 V-cycle equals the FP64 one to FP32 round-off when the
-    mapping degree is at most 2; at degree 3 the FP32 levels see the
-    mapping's degree-2 interpolant, a small change of the preconditioner."""
-    case = build_case(HillParams(nx=32, nz=16, degree=4, cfl=5.0,
+    mapping and stage A^{-1} through shared memory: the FP32 V-cycle equals
+    the FP64 one to FP32 round-off when the mapping degree is at most 2; at
+    degree 3 the FP32 levels see the mapping's degree-2 interpolant, a small
+    change of the preconditioner."""
+    case = build_case(HillParams(nx=32, nz=16, degree=degree, cfl=5.0,
                                  mapping_degree=mapping_degree))
     op, rng = schur_op(case)
     b = dev(rng.standard_normal(op.n_scalar))
