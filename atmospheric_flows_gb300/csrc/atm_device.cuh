@@ -422,10 +422,14 @@ __device__ __forceinline__ int hanging_mask(const MeshT<T> &mesh, int c) {
 // With HG, a face of code 1/2 reads the neighbour at the shifted points; a face
 // of code 3 is integrated on its two subfaces, with the s = 1 values going to
 // fhc (same layout).  Without HG the loop is the conforming one.
+//
+// `fgc` (optional): this cell's conforming face geometry [4][3][NQ] already
+// staged in shared memory, read instead of mesh.fgeo.
 template <int K, int NC, bool HG, typename T, typename Body>
 __device__ __forceinline__ void face_terms(const MeshT<T> &mesh, int c, int col,
                                            const T (&Sx)[K + 1], T *__restrict__ fbc,
-                                           T *__restrict__ fhc, Body &&body) {
+                                           T *__restrict__ fhc, Body &&body,
+                                           const T *__restrict__ fgc = nullptr) {
   constexpr int NQ = 2 * K + 1;
   // the four neighbours and their faces in two 16-byte loads; FP32 (latency
   // bound) unrolls the faces so that their loads overlap
@@ -438,7 +442,7 @@ __device__ __forceinline__ void face_terms(const MeshT<T> &mesh, int c, int col,
     const int code = HG && nb >= 0 ? (nfc >> 2) : 0;
     T val[NC];
     if (code == 0) {
-      const T *fg = mesh.fgeo + ((long)c * 4 + f) * 3 * NQ;
+      const T *fg = fgc ? fgc + f * 3 * NQ : mesh.fgeo + ((long)c * 4 + f) * 3 * NQ;
       body(f, nb, nfc & 3, fg[col], fg[NQ + col], fg[2 * NQ + col], Sx, Sx, val);
 #pragma unroll
       for (int comp = 0; comp < NC; ++comp) fbc[comp * 4 * NQ + f * NQ + col] = val[comp];
@@ -547,6 +551,10 @@ inline long ainv_stride_rt(int k, size_t elem) {
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() {
   asm volatile("cp.async.commit_group;\n" ::: "memory");

@@ -169,18 +169,49 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS, sizeof(T) == 4 ? 4 : 1)
   constexpr T HG_ = GAS_GAMMA / (GAS_GAMMA - T(1.0));  // enthalpy factor
   // sign of the C contribution in dst
   constexpr T SC = WITH_D ? -T(1.0) : T(1.0);
+  // FP32 on conforming levels (latency bound): the block's own face
+  // geometry, p_fix traces and quadrature values, and in MODE 4 its rhs,
+  // invd and d, are contiguous; they are copied into shared memory with
+  // cp.async at the start instead of being loaded thread by thread
+  constexpr bool STG = sizeof(T) == 4 && !HG;
+  constexpr int FGS = 12 * NQ, PFS = 4 * NQ;  // multiples of 4 values
+  constexpr int NV = MODE == 4 ? 3 : 0;
+  constexpr int STS = FGS + PFS + NQ2 + NV * NN2;  // staged values per cell
   extern __shared__ __align__(16) unsigned char sm_raw[];
   T *sm = reinterpret_cast<T *>(sm_raw);
-  T *tiles = sm;
+  T *sfg = sm;                   // [CPB][FGS] (STG)
+  T *spf = sfg + CPB * FGS;      // [CPB][PFS]
+  T *spq = spf + CPB * PFS;      // [CPB][NQ2]
+  T *svec = spq + CPB * NQ2;     // [NV][CPB][NN2]: rhs, invd, d
+  T *tiles = sm + (STG ? (CPB * STS + 3) / 4 * 4 : 0);
   T *xab = tiles + CPB * NT * NN2;
   T *fb = xab + CPB * 2 * NN * NQ;
   T *fh = fb + CPB * 4 * NQ;  // subface-1 values (HG)
   const int tid = threadIdx.x, lc = tid / NQ, col = tid - lc * NQ;
   const int c0 = blockIdx.x * CPB;
   const int cnt = min(CPB, mesh.nc - c0);
+  if constexpr (STG) {
+    // cells c0 .. c0+cnt-1; fgeo and pff blocks are 16-byte aligned
+    const T *gfg = mesh.fgeo + (long)c0 * FGS, *gpf = pff + (long)c0 * PFS;
+    for (int e = tid; e < cnt * FGS / 4; e += blockDim.x) cp_async16(sfg + 4 * e, gfg + 4 * e);
+    for (int e = tid; e < cnt * PFS / 4; e += blockDim.x) cp_async16(spf + 4 * e, gpf + 4 * e);
+    const T *gpq = pfq + (long)c0 * NQ2;
+    for (int e = tid; e < cnt * NQ2; e += blockDim.x) cp_async4(spq + e, gpq + e);
+    if constexpr (NV > 0) {
+      const T *vs[3] = {ch.rhs, invd, ch.d};
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        const T *g = vs[v] + (long)c0 * NN2;
+        T *d = svec + v * CPB * NN2;
+        for (int e = tid; e < cnt * NN2; e += blockDim.x) cp_async4(d + e, g + e);
+      }
+    }
+    cp_async_commit();
+  }
   load_tiles<K>(tiles, NT, 0, w, 2, c0, cnt);
   if (PT) load_tiles<K>(tiles, NT, 2, pfix, 1, c0, cnt);
   if (WITH_D) load_tiles<K>(tiles, NT, TP, p, 1, c0, cnt);
+  if constexpr (STG) cp_async_wait_all();
   __syncthreads();
   const bool active = lc < cnt;
   const int c = c0 + lc;
@@ -195,8 +226,9 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS, sizeof(T) == 4 ? 4 : 1)
     if (PT) {
       eval_col<K>(tl + 2 * NN2, Sx, pf);
     } else {
+      const T *pq = STG ? spq + lc * NQ2 : pfq + (long)c * NQ2;
 #pragma unroll
-      for (int qz = 0; qz < NQ; ++qz) pf[qz] = pfq[(long)c * NQ2 + qz * NQ + col];
+      for (int qz = 0; qz < NQ; ++qz) pf[qz] = pq[qz * NQ + col];
     }
     if (WITH_D) eval_col<K>(tl + TP * NN2, Sx, pv);
     const GeoCol<K, T> G(mesh, c, col);
@@ -228,7 +260,7 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS, sizeof(T) == 4 ? 4 : 1)
         pfp = face_val<K>(tl + 2 * NN2, f, Ro);
         pfm = face_val<K>(pfix + (long)nb * NN2, nf, Rn);
       } else {  // conforming: face point col of both sides coincide
-        pfp = pff[((long)c * 4 + f) * NQ + col];
+        pfp = STG ? spf[lc * PFS + f * NQ + col] : pff[((long)c * 4 + f) * NQ + col];
         pfm = pff[((long)nb * 4 + nf) * NQ + col];
       }
       const T av0 = T(0.5) * HG_ * (pfp * wxp + pfm * wxm);
@@ -236,7 +268,7 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS, sizeof(T) == 4 ? 4 : 1)
       const T lam = fmax(fabs(wxp * n0 + wzp * n1), fabs(wxm * n0 + wzm * n1));
       const T je = T(1.0) / GM1 * (pfp - pfm);
       val[0] = SC * cC * ((av0 * n0 + av1 * n1) + T(0.5) * lam * je) * jxw;
-    });
+    }, STG ? sfg + lc * FGS : nullptr);
   }
   __syncthreads();
   if (active && col < NN) {
@@ -255,10 +287,22 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS, sizeof(T) == 4 ? 4 : 1)
         d[i] -= out[iz];
       } else if (MODE == 4) {
         const long g = (long)c * NN2 + i;
-        const T r = ch.rhs[g] - out[iz];
-        const T dk = (ch.first ? T(0) : ch.a * ch.d[g]) + ch.b * invd[g] * r;
+        T rh, dd, iv, xx;
+        if constexpr (STG) {  // staged rhs, invd, d; x = p is the tile TP
+          rh = svec[lc * NN2 + i];
+          iv = svec[(CPB + lc) * NN2 + i];
+          dd = svec[(2 * CPB + lc) * NN2 + i];
+          xx = tiles[(lc * NT + TP) * NN2 + i];
+        } else {
+          rh = ch.rhs[g];
+          iv = invd[g];
+          dd = ch.d[g];
+          xx = ch.x[g];
+        }
+        const T r = rh - out[iz];
+        const T dk = (ch.first ? T(0) : ch.a * dd) + ch.b * iv * r;
         ch.d[g] = dk;
-        ch.x[g] = ch.x[g] + dk;
+        ch.x[g] = xx + dk;
       } else {
         d[i] = out[iz];
       }
@@ -354,7 +398,12 @@ int CD_launch(const OpView<T> &v, T *dst, const T *w, const T *p, T cC, int mode
   using C = Cfg<K>;
   auto launch = [&](int cpb) -> cudaError_t {
     const int grid = (v.nc + cpb - 1) / cpb, th = cpb * C::NQ;
-    const size_t sm = smem_bytes<K, T>(cpb, 4, 1, HG);
+    // plus the FP32 conforming staging buffer (k_CD: STG)
+    const size_t stg = (sizeof(T) == 4 && !HG)
+                           ? sizeof(T) * (((size_t)cpb * (16 * C::NQ + C::NQ2 +
+                                                          (mode == 4 ? 3 * C::NN2 : 0)) + 3) / 4 * 4)
+                           : 0;
+    const size_t sm = smem_bytes<K, T>(cpb, 4, 1, HG) + stg;
     void (*fn)(T *, const T *, const T *, const T *, const T *, const T *, T, const T *,
                MeshT<T>, ChebArgs<T>) =
         mode == 0 ? k_CD<K, 0, T, HG>
