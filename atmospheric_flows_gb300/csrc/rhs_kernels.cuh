@@ -266,6 +266,12 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
   constexpr int NG = (ST == 1) ? 2 : 3;
   constexpr int NT = 4 * ST + 3;
   constexpr double GM1 = GAS_GAMMA - 1.0;
+  // The reference forms E = p / ((gamma-1) rho) + Ma^2 |u|^2 / 2 and then
+  // only uses rho E and rho (E - Ma^2 |u|^2 / 2) + p.  Those are
+  // p / (gamma-1) + rho Ma^2 |u|^2 / 2 and gamma / (gamma-1) p: the division
+  // by rho cancels, and the kernel forms the products directly (no FP64
+  // division per point; the values agree to rounding).
+  constexpr double IG = 1.0 / GM1, HGF = GAS_GAMMA / GM1;
   extern __shared__ double sm[];
   double *tiles = sm;
   double *xab = tiles + CPB * NT * NN2;
@@ -307,11 +313,10 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
 #pragma unroll
       for (int q = 0; q < NQ; ++q) {
         const double uu = ux[q] * ux[q] + uz[q] * uz[q];
-        const double E = 1.0 / GM1 * (p[q] / r[q]) + 0.5 * M2 * uu;
-        if (j == 0) v[q] += r[q] * E;
+        if (j == 0) v[q] += IG * p[q] + 0.5 * M2 * uu * r[q];  // rho E
         v[q] -= wgrav * r[q] * uz[q];
         const double kin = wk * uu * r[q];
-        const double ent = we * (r[q] * (E - 0.5 * M2 * uu) + p[q]);
+        const double ent = we * HGF * p[q];  // rho (E - Ma^2 |u|^2 / 2) + p
         gx[q] += kin * ux[q] + ent * ux[q];
         gz[q] += kin * uz[q] + ent * uz[q];
       }
@@ -365,16 +370,14 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
         const double uup = uxp * uxp + uzp * uzp, uum = uxm * uxm + uzm * uzm;
         const double unp = uxp * n0 + uzp * n1, unm = uxm * n0 + uzm * n1;
         const double akin = 0.5 * (0.5 * uup * rp * unp + 0.5 * uum * rm * unm);
-        const double Ep = 1.0 / GM1 * pp / rp + 0.5 * M2 * uup;
-        const double Em = 1.0 / GM1 * pm / rm + 0.5 * M2 * uum;
-        const double hp = (Ep - 0.5 * M2 * uup) * rp + pp;
-        const double hm = (Em - 0.5 * M2 * uum) * rm + pm;
+        // enthalpy rho (E - Ma^2 |u|^2 / 2) + p of each side
+        const double hp = HGF * pp, hm = HGF * pm;
         const double aent = 0.5 * (hp * unp + hm * unm);
         const double lam = fmax(fabs(unp), fabs(unm));
         const double wa = co.ca[j] * co.dt;
         if (ST == 3) {
           // stage 3 jumps the total rho E (euler_operator.h:1290,1313,1336)
-          const double jE = rp * Ep - rm * Em;
+          const double jE = IG * (pp - pm) + 0.5 * M2 * (rp * uup - rm * uum);
           flux += wa * M2 * akin + wa * aent + wa * 0.5 * lam * jE;
         } else {
           // stage 2 keeps the reference's mixed kinetic jump for tmp_2
@@ -383,7 +386,7 @@ __global__ void __launch_bounds__(Cfg<K>::MAX_THREADS)
                                   ? rp * 0.5 * (uxp * ux0p + uzp * uz0p) -
                                         rm * 0.5 * (uxm * ux0m + uzm * uz0m)
                                   : rp * 0.5 * uup - rm * 0.5 * uum;
-          const double je = rp * (Ep - 0.5 * M2 * uup) - rm * (Em - 0.5 * M2 * uum);
+          const double je = IG * (pp - pm);  // jump of rho (E - Ma^2 |u|^2 / 2)
           flux += wa * M2 * (akin + 0.5 * lam * jkin) +
                   co.ct[j] * co.dt * (aent + 0.5 * lam * je);
         }

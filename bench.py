@@ -503,7 +503,9 @@ def run_gb300(args):
                          "frac": tflops / FP64_PEAK_TFLOPS,
                          "note": "FP64 FMA pipe is the binding limit on GB300"},
                 "families": {fams[i]: {"ms": ms[i], "launches": int(cnt[i]),
-                                       "share": ms[i] / max(total_ms, 1e-30)}
+                                       "share": ms[i] / max(total_ms, 1e-30),
+                                       "gbs": byt[i] / max(ms[i] * 1e-3, 1e-30) / 1e9,
+                                       "fp64_tflops": flp[i] / max(ms[i] * 1e-3, 1e-30) / 1e12}
                              for i in range(len(fams)) if cnt[i]}}
     cpu = None
     if not args.no_cpu_baseline:
