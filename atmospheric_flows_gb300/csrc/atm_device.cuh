@@ -662,6 +662,28 @@ struct GeoCol<K, float> {
   }
 };
 
+// Let kernel `fn` use up to the device's opt-in maximum of dynamic shared
+// memory when a launch needs more than the default 48 KB.  The limit is set
+// to that maximum, always the same value: host threads launching the same
+// kernel with different block shapes (serving members, the autotuner) must
+// never lower each other's limit between setting it and launching.
+template <typename F>
+inline cudaError_t allow_smem(F fn, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  static int cap[64] = {0};  // per device; a benign race writes the same value
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  int mx = dev >= 0 && dev < 64 ? cap[dev] : 0;
+  if (mx == 0) {
+    e = cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return e;
+    if (dev >= 0 && dev < 64) cap[dev] = mx;
+  }
+  if (bytes > (size_t)mx) return cudaErrorInvalidValue;
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+}
+
 // tiles, x-contraction exchange, face values [, subface-1 face values]
 template <int K, typename T = double>
 inline size_t smem_bytes(int cpb, int n_tiles, int ncomp_out, bool hg = false) {

@@ -320,9 +320,7 @@ int invdiag_launch(const OpView<T> &v, T *out, int ncomp, const T *weight, T sca
 template <int K, typename T>
 int block_inverse_launch(const OpView<T> &v, T *out, const T *weight) {
   const size_t sm = BlockInvCfg<K>::template smem<T>();
-  if (sm > 48 * 1024)
-    ATM_CUDA(cudaFuncSetAttribute(k_block_inverse<K, T>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  ATM_CUDA(allow_smem(k_block_inverse<K, T>, sm));
   const int grid = (v.nc + BI_WARPS - 1) / BI_WARPS;
   k_block_inverse<K, T><<<grid, 32 * BI_WARPS, sm, v.st>>>(out, weight, v.mesh);
   ATM_CHECK_LAUNCH("k_block_inverse");

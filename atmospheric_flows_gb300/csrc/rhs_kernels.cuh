@@ -434,10 +434,7 @@ int rhs_launch(const atm_ctx &c, int stage, double *dst, const double *const *sr
   const int ncomp = kind == 1 ? 2 : 1;
   auto launch = [&](int cpb) -> cudaError_t {
     const size_t sm = smem_bytes<K>(cpb, ntile, ncomp, HG);
-    if (sm > 48 * 1024) {
-      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      if (e != cudaSuccess) return e;
-    }
+    if (cudaError_t e = allow_smem(fn, sm); e != cudaSuccess) return e;
     fn<<<(c.nc + cpb - 1) / cpb, cpb * C::NQ, sm, c.stream>>>(dst, sp, co, c.mesh);
     return cudaGetLastError();
   };

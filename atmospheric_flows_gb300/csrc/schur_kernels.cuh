@@ -365,10 +365,7 @@ int B_launch(const OpView<T> &v, T *dst, const T *p, T cB, int mode) {
                       (mode == 2 && sizeof(T) == 4 ? sizeof(T) * cpb * ainv_stride<K, T>() : 0);
     void (*fn)(T *, const T *, T, const T *, MeshT<T>) =
         mode == 0 ? k_B<K, 0, T, HG> : (mode == 1 ? k_B<K, 1, T, HG> : k_B<K, 2, T, HG>);
-    if (sm > 48 * 1024) {
-      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      if (e != cudaSuccess) return e;
-    }
+    if (cudaError_t e = allow_smem(fn, sm); e != cudaSuccess) return e;
     fn<<<grid, th, sm, v.st>>>(dst, p, cB, v.ainv, v.mesh);
     return cudaGetLastError();
   };
@@ -411,10 +408,7 @@ int CD_launch(const OpView<T> &v, T *dst, const T *w, const T *p, T cC, int mode
         : mode == 2 ? k_CD<K, 2, T, HG>
         : mode == 3 ? k_CD<K, 3, T, HG>
                     : k_CD<K, 4, T, HG>;
-    if (sm > 48 * 1024) {
-      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      if (e != cudaSuccess) return e;
-    }
+    if (cudaError_t e = allow_smem(fn, sm); e != cudaSuccess) return e;
     fn<<<grid, th, sm, v.st>>>(dst, w, p, pfix, v.pfq, v.pff, cC, v.invd, v.mesh, ch);
     return cudaGetLastError();
   };

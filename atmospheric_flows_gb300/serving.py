@@ -13,12 +13,15 @@ under continuous batching:
   * members advance with the mixed-precision solver (FP64 state, FGMRES
     with an FP32 multigrid preconditioner) unless told otherwise;
   * with batch_size > 1, requests waiting at admission that share the
-    degree and the solver (any mesh sizes) are concatenated into one context
-    (batch.py): every kernel launch then covers all of their cells, while
-    each member keeps its own time step and its own Krylov and Picard stops.
-    A batch runs until its longest member is done; each member's result is
-    taken when its own step count is reached, and a member that fails is
-    reported alone.
+    degree and the solver are concatenated into one context (batch.py):
+    every kernel launch then covers all of their cells, while each member
+    keeps its own time step and its own Krylov and Picard stops.  Only small
+    members are batched (at most batch_max_cells cells each, 3200 by
+    default): their own launches leave most of the GPU idle, while a large
+    member fills it alone and, batched, would make its co-residents run its
+    Krylov iterations.  A batch runs until its longest member is done; each
+    member's result is taken when its own step count is reached, and a
+    member that fails is reported alone.
 
 Unbatched members never share device data or reductions, so a member's
 result is bitwise the same alone and in a mix (the kernels are
@@ -117,12 +120,13 @@ class Server:
     """Continuous-batching scheduler for ensemble members on one GPU."""
 
     def __init__(self, hbm_budget=150e9, max_running=32, chunk_steps=10, keep_state=False,
-                 batch_size=1):
+                 batch_size=1, batch_max_cells=3200):
         self.budget = float(hbm_budget)
         self.max_running = int(max_running)
         self.chunk = int(chunk_steps)
         self.keep_state = keep_state
         self.batch_size = int(batch_size)
+        self.batch_max_cells = int(batch_max_cells)
         self.batches = []  # member count of every batch started
         self._lock = threading.Condition()
         self._in_use = 0.0
@@ -264,12 +268,16 @@ class Server:
                                                      head.steps, 0, "rejected: over budget"))
                     continue
                 group = [head]
-                if self.batch_size > 1:
+
+                def small(r):
+                    return r.params.nx * r.params.nz <= self.batch_max_cells
+
+                if self.batch_size > 1 and small(head):
                     key = (batch_key(head.params), head.precision, head.eps)
                     for r in queue[1:]:
                         if len(group) >= self.batch_size:
                             break
-                        if (batch_key(r.params), r.precision, r.eps) == key:
+                        if small(r) and (batch_key(r.params), r.precision, r.eps) == key:
                             group.append(r)
                 nb = sum(member_bytes(r.params, r.precision) for r in group)
                 while len(group) > 1 and nb > self.budget:

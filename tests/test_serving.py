@@ -239,3 +239,35 @@ def test_scheduler_does_not_mix_keys():
     srv.run(a + b)
     for g in srv.groups:
         assert all(i < 100 for i in g) or all(i >= 100 for i in g)
+
+
+def test_scheduler_batches_small_members_only():
+    """A member larger than batch_max_cells runs alone: it fills the GPU by
+    itself, and batched it would make its co-residents run its iterations."""
+    small = make_requests(n=6, rate=1e6, seed=7, meshes=((40, 20),), degrees=(3,))
+    large = make_requests(n=4, rate=1e6, seed=8, meshes=((160, 80),), degrees=(3,))
+    for i, r in enumerate(large):
+        r.request_id = 100 + i
+    srv = _FakeServer(batch_size=4)
+    srv.run(small + large)
+    assert max(len(g) for g in srv.groups) > 1
+    for g in srv.groups:
+        assert len(g) == 1 or all(i < 100 for i in g)
+
+
+@pytest.mark.gpu
+def test_batched_mix_of_degrees_and_meshes_completes(cuda_ok):
+    """Members of every degree 2-5 on meshes up to 160x80 (those up to 80x40
+    batched) served at once from concurrent host threads: every member
+    completes.  Members of one degree
+    launch the same kernels with block shapes of their own (the autotuner
+    tunes per mesh size); a kernel's shared-memory limit is raised once to
+    the device maximum, never set per launch, so one thread cannot lower it
+    under another's launch."""
+    reqs = make_requests(n=24, rate=1e6, seed=11, meshes=((40, 20), (80, 40), (160, 80)),
+                         degrees=(2, 3, 4, 5), steps_range=(3, 6))
+    srv = Server(batch_size=4, max_running=16)
+    res = srv.run(reqs)
+    s = summarize(res, srv.makespan)
+    assert s["completed"] == 24 and not s["failed"], s
+    assert max(srv.batches) > 1
