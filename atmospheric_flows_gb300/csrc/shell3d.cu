@@ -94,123 +94,159 @@ __device__ __forceinline__ void to_ref(const double *cgq, const double *P, doubl
   for (int e = 0; e < 3; ++e) Gr[e] = cgq[3 * e] * P[0] + cgq[3 * e + 1] * P[1] + cgq[3 * e + 2] * P[2];
 }
 
+// Every face-integral kernel runs one warp per cell (CELLS3 cells per
+// block): lanes take the 27 quadrature points and the 54 face points of the
+// cell, write their integrands to shared memory, and one lane per output
+// node and component sums them against the basis.  One thread per cell
+// would leave 6144 cells on a third of the SMs with long serial chains.
+constexpr int CELLS3 = 4;
+
+// Copy n values per cell of a field with ncomp components into shared memory:
+// dst[comp][i] for the cell's components comp < ncomp (lanes of one warp).
+__device__ __forceinline__ void tile3(double *dst, const double *src, int c, int ncomp,
+                                      int lane) {
+  for (int e = lane; e < ncomp * NN; e += 32) dst[e] = src[(long)c * ncomp * NN + e];
+}
+
+// sum over the cell's points of V_q phi_i + Gr_q . grad phi_i, then over the
+// face points of F_fq phi_i (the order of the one-thread version)
+__device__ __forceinline__ double gather3(const double (*sv)[4], const double (*sf)[NF], int i) {
+  double o = 0.0;
+  for (int q = 0; q < NQ; ++q)
+    o += sv[q][0] * c_phi[q][i] + sv[q][1] * c_dphi[q][i][0] + sv[q][2] * c_dphi[q][i][1] +
+         sv[q][3] * c_dphi[q][i][2];
+  for (int f = 0; f < 6; ++f)
+#pragma unroll
+    for (int q = 0; q < NF; ++q) o += sf[f][q] * c_fphi[f][q][i];
+  return o;
+}
+
 // ------------------------------------------------------------- rho rhs --
 // euler_operator.h:344-712; src = (rho^(j), u^(j)) for j < nst
-__global__ void k3_rhs_rho(double *__restrict__ dst, SrcPtrs src, Coef3 co, Geo3 g) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= g.nc) return;
-  double out[NN] = {0};
-  double rt[3][NN], ut[3][3][NN];
-  for (int j = 0; j < co.nst; ++j) {
-    load8(src.p[2 * j], c, 1, 0, rt[j]);
-    for (int d = 0; d < 3; ++d) load8(src.p[2 * j + 1], c, 3, d, ut[j][d]);
-  }
-  double V[NQ], Gr[NQ][3];
-  for (int q = 0; q < NQ; ++q) {
-    const double *cq = g.cg + ((long)c * NQ + q) * 13;
-    V[q] = at_q(rt[0], q) * cq[9];
-    double P[3] = {0, 0, 0};
+__global__ void __launch_bounds__(32 * CELLS3)
+    k3_rhs_rho(double *__restrict__ dst, SrcPtrs src, Coef3 co, Geo3 g) {
+  __shared__ double srt[CELLS3][3][NN], sut[CELLS3][3][3][NN];
+  __shared__ double sv[CELLS3][NQ][4], sf[CELLS3][6][NF];
+  const int lc = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * CELLS3 + lc;
+  const bool active = c < g.nc;
+  if (active)
     for (int j = 0; j < co.nst; ++j) {
-      const double r = at_q(rt[j], q), w = co.ca[j] * co.dt * r;
-      for (int d = 0; d < 3; ++d) P[d] += w * at_q(ut[j][d], q);
+      tile3(srt[lc][j], src.p[2 * j], c, 1, lane);
+      tile3(&sut[lc][j][0][0], src.p[2 * j + 1], c, 3, lane);
     }
-    to_ref(cq, P, Gr[q]);
-  }
-  integ(out, V, Gr);
-  for (int f = 0; f < 6; ++f) {
-    if (g.nbr[c * 6 + f] < 0) continue;  // no boundary term (euler_operator.h:111-114)
-    double F[NF];
-    for (int q = 0; q < NF; ++q) {
-      const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
-      double flux = 0.0;
+  __syncthreads();
+  if (active) {
+    if (lane < NQ) {
+      const int q = lane;
+      const double *cq = g.cg + ((long)c * NQ + q) * 13;
+      sv[lc][q][0] = at_q(srt[lc][0], q) * cq[9];
+      double P[3] = {0, 0, 0};
       for (int j = 0; j < co.nst; ++j) {
-        const double ro = at_face(rt[j], f, q), rn = nb_face(g, src.p[2 * j], 1, 0, c, f, q);
-        double avg = 0.0, uno = 0.0, unn = 0.0;
-        for (int d = 0; d < 3; ++d) {
-          const double uo = at_face(ut[j][d], f, q);
-          const double un = nb_face(g, src.p[2 * j + 1], 3, d, c, f, q);
-          avg += 0.5 * (ro * uo + rn * un) * fq[d];
-          uno += uo * fq[d];
-          unn += un * fq[d];
-        }
-        flux += co.ca[j] * co.dt * (avg + 0.5 * fmax(fabs(uno), fabs(unn)) * (ro - rn));
+        const double r = at_q(srt[lc][j], q), w = co.ca[j] * co.dt * r;
+        for (int d = 0; d < 3; ++d) P[d] += w * at_q(sut[lc][j][d], q);
       }
-      F[q] = -flux * fq[3];
+      to_ref(cq, P, &sv[lc][q][1]);
     }
-    for (int q = 0; q < NF; ++q)
-#pragma unroll
-      for (int i = 0; i < NN; ++i) out[i] += F[q] * c_fphi[f][q][i];
+    for (int e = lane; e < 6 * NF; e += 32) {
+      const int f = e / NF, q = e - f * NF;
+      double F = 0.0;
+      if (g.nbr[c * 6 + f] >= 0) {  // no boundary term (euler_operator.h:111-114)
+        const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
+        double flux = 0.0;
+        for (int j = 0; j < co.nst; ++j) {
+          const double ro = at_face(srt[lc][j], f, q), rn = nb_face(g, src.p[2 * j], 1, 0, c, f, q);
+          double avg = 0.0, uno = 0.0, unn = 0.0;
+          for (int d = 0; d < 3; ++d) {
+            const double uo = at_face(sut[lc][j][d], f, q);
+            const double un = nb_face(g, src.p[2 * j + 1], 3, d, c, f, q);
+            avg += 0.5 * (ro * uo + rn * un) * fq[d];
+            uno += uo * fq[d];
+            unn += un * fq[d];
+          }
+          flux += co.ca[j] * co.dt * (avg + 0.5 * fmax(fabs(uno), fabs(unn)) * (ro - rn));
+        }
+        F = -flux * fq[3];
+      }
+      sf[lc][f][q] = F;
+    }
   }
-#pragma unroll
-  for (int i = 0; i < NN; ++i) dst[(long)c * NN + i] = out[i];
+  __syncthreads();
+  if (active && lane < NN) dst[(long)c * NN + lane] = gather3(sv[lc], sf[lc], lane);
 }
 
 // ------------------------------------------------------------ momentum --
 // euler_operator.h:1622-2305; src = (rho, u, p)^(j) for j < nst, then the
 // densities of the gravity terms at gsrc[0..ng)
-__global__ void k3_rhs_vel(double *__restrict__ dst, SrcPtrs src, SrcPtrs gsrc, Coef3 co,
-                           Geo3 g) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= g.nc) return;
+__global__ void __launch_bounds__(32 * CELLS3)
+    k3_rhs_vel(double *__restrict__ dst, SrcPtrs src, SrcPtrs gsrc, Coef3 co, Geo3 g) {
+  __shared__ double srt[CELLS3][3][NN], sut[CELLS3][3][3][NN], spt[CELLS3][3][NN];
+  __shared__ double sgt[CELLS3][3][NN];
+  __shared__ double sv[CELLS3][3][NQ][4], sf[CELLS3][3][6][NF];  // per component d
+  const int lc = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * CELLS3 + lc;
+  const bool active = c < g.nc;
   const double iM2 = 1.0 / (co.Ma * co.Ma), iF2 = 1.0 / (co.Fr * co.Fr);
-  double rt[3][NN], ut[3][3][NN], pt[3][NN], gt[3][NN];
-  for (int j = 0; j < co.nst; ++j) {
-    load8(src.p[3 * j], c, 1, 0, rt[j]);
-    for (int d = 0; d < 3; ++d) load8(src.p[3 * j + 1], c, 3, d, ut[j][d]);
-    load8(src.p[3 * j + 2], c, 1, 0, pt[j]);
+  if (active) {
+    for (int j = 0; j < co.nst; ++j) {
+      tile3(srt[lc][j], src.p[3 * j], c, 1, lane);
+      tile3(&sut[lc][j][0][0], src.p[3 * j + 1], c, 3, lane);
+      tile3(spt[lc][j], src.p[3 * j + 2], c, 1, lane);
+    }
+    for (int j = 0; j < co.ng; ++j) tile3(sgt[lc][j], gsrc.p[j], c, 1, lane);
   }
-  for (int j = 0; j < co.ng; ++j) load8(gsrc.p[j], c, 1, 0, gt[j]);
-  for (int d = 0; d < 3; ++d) {
-    double out[NN] = {0};
-    double V[NQ], Gr[NQ][3];
-    for (int q = 0; q < NQ; ++q) {
+  __syncthreads();
+  if (active) {
+    if (lane < NQ) {
+      const int q = lane;
       const double *cq = g.cg + ((long)c * NQ + q) * 13;
-      double v = at_q(rt[0], q) * at_q(ut[0][d], q);
-      for (int j = 0; j < co.ng; ++j) v -= co.cg[j] * co.dt * iF2 * at_q(gt[j], q) * cq[10 + d];
-      V[q] = v * cq[9];
-      double P[3] = {0, 0, 0};
-      for (int j = 0; j < co.nst; ++j) {
-        const double ru = co.ca[j] * co.dt * at_q(rt[j], q) * at_q(ut[j][d], q);
-        for (int k = 0; k < 3; ++k) P[k] += ru * at_q(ut[j][k], q);
-        P[d] += co.ct[j] * co.dt * iM2 * at_q(pt[j], q);
-      }
-      to_ref(cq, P, Gr[q]);  // the geometry factors carry JxW
-    }
-    integ(out, V, Gr);
-    for (int f = 0; f < 6; ++f) {
-      const bool wall = g.nbr[c * 6 + f] < 0;
-      double F[NF];
-      for (int q = 0; q < NF; ++q) {
-        const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
-        double fl = 0.0;
+      for (int d = 0; d < 3; ++d) {
+        double v = at_q(srt[lc][0], q) * at_q(sut[lc][0][d], q);
+        for (int j = 0; j < co.ng; ++j)
+          v -= co.cg[j] * co.dt * iF2 * at_q(sgt[lc][j], q) * cq[10 + d];
+        sv[lc][d][q][0] = v * cq[9];
+        double P[3] = {0, 0, 0};
         for (int j = 0; j < co.nst; ++j) {
-          const double po = at_face(pt[j], f, q);
-          if (wall) {  // p_D = p (euler_operator.h:2189-2305)
-            fl += co.ct[j] * co.dt * iM2 * 0.5 * (po + po) * fq[d];
-            continue;
-          }
-          const double ro = at_face(rt[j], f, q), rn = nb_face(g, src.p[3 * j], 1, 0, c, f, q);
-          const double pn = nb_face(g, src.p[3 * j + 2], 1, 0, c, f, q);
-          double uo[3], un[3], uno = 0.0, unn = 0.0;
-          for (int k = 0; k < 3; ++k) {
-            uo[k] = at_face(ut[j][k], f, q);
-            un[k] = nb_face(g, src.p[3 * j + 1], 3, k, c, f, q);
-            uno += uo[k] * fq[k];
-            unn += un[k] * fq[k];
-          }
-          const double lam = fmax(fabs(uno), fabs(unn));
-          fl += co.ca[j] * co.dt * 0.5 * (ro * uo[d] * uno + rn * un[d] * unn) +
-                co.ct[j] * co.dt * iM2 * 0.5 * (po + pn) * fq[d] +
-                co.ca[j] * co.dt * 0.5 * lam * (ro * uo[d] - rn * un[d]);
+          const double ru = co.ca[j] * co.dt * at_q(srt[lc][j], q) * at_q(sut[lc][j][d], q);
+          for (int k = 0; k < 3; ++k) P[k] += ru * at_q(sut[lc][j][k], q);
+          P[d] += co.ct[j] * co.dt * iM2 * at_q(spt[lc][j], q);
         }
-        F[q] = -fl * fq[3];
+        to_ref(cq, P, &sv[lc][d][q][1]);  // the geometry factors carry JxW
       }
-      for (int q = 0; q < NF; ++q)
-#pragma unroll
-        for (int i = 0; i < NN; ++i) out[i] += F[q] * c_fphi[f][q][i];
     }
-#pragma unroll
-    for (int i = 0; i < NN; ++i) dst[((long)c * 3 + d) * NN + i] = out[i];
+    for (int e = lane; e < 6 * NF; e += 32) {
+      const int f = e / NF, q = e - f * NF;
+      const bool wall = g.nbr[c * 6 + f] < 0;
+      const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
+      double fl[3] = {0, 0, 0};
+      for (int j = 0; j < co.nst; ++j) {
+        const double po = at_face(spt[lc][j], f, q);
+        if (wall) {  // p_D = p (euler_operator.h:2189-2305)
+          for (int d = 0; d < 3; ++d) fl[d] += co.ct[j] * co.dt * iM2 * 0.5 * (po + po) * fq[d];
+          continue;
+        }
+        const double ro = at_face(srt[lc][j], f, q), rn = nb_face(g, src.p[3 * j], 1, 0, c, f, q);
+        const double pn = nb_face(g, src.p[3 * j + 2], 1, 0, c, f, q);
+        double uo[3], un[3], uno = 0.0, unn = 0.0;
+        for (int k = 0; k < 3; ++k) {
+          uo[k] = at_face(sut[lc][j][k], f, q);
+          un[k] = nb_face(g, src.p[3 * j + 1], 3, k, c, f, q);
+          uno += uo[k] * fq[k];
+          unn += un[k] * fq[k];
+        }
+        const double lam = fmax(fabs(uno), fabs(unn));
+        for (int d = 0; d < 3; ++d)
+          fl[d] += co.ca[j] * co.dt * 0.5 * (ro * uo[d] * uno + rn * un[d] * unn) +
+                   co.ct[j] * co.dt * iM2 * 0.5 * (po + pn) * fq[d] +
+                   co.ca[j] * co.dt * 0.5 * lam * (ro * uo[d] - rn * un[d]);
+      }
+      for (int d = 0; d < 3; ++d) sf[lc][d][f][q] = -fl[d] * fq[3];
+    }
+  }
+  __syncthreads();
+  if (active && lane < 3 * NN) {
+    const int d = lane / NN, i = lane - d * NN;
+    dst[((long)c * 3 + d) * NN + i] = gather3(sv[lc][d], sf[lc][d], i);
   }
 }
 
@@ -218,212 +254,252 @@ __global__ void k3_rhs_vel(double *__restrict__ dst, SrcPtrs src, SrcPtrs gsrc, 
 // euler_operator.h:745-1381 with the radial gravity work (:790-811), the
 // stage-2 kinetic jump mixing in u_old (:1182-1183) and the stage-3 total
 // rho E jump (:1290-1336).  src = (rho, u, p)^(j); gsrc = gravity densities
-// and velocities (rho, u)^(j) for j < ng, then the kinetic (rho, u).
-__global__ void k3_rhs_pres(double *__restrict__ dst, SrcPtrs src, SrcPtrs gsrc, Coef3 co,
-                            int hstage, Geo3 g) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= g.nc) return;
-  const double gm1 = GAS_GAMMA - 1.0, M2 = co.Ma * co.Ma, iF2 = 1.0 / (co.Fr * co.Fr);
-  double rt[3][NN], ut[3][3][NN], pt[3][NN];
-  for (int j = 0; j < co.nst; ++j) {
-    load8(src.p[3 * j], c, 1, 0, rt[j]);
-    for (int d = 0; d < 3; ++d) load8(src.p[3 * j + 1], c, 3, d, ut[j][d]);
-    load8(src.p[3 * j + 2], c, 1, 0, pt[j]);
+// and velocities (rho, u)^(j) for j < ng, then the kinetic (rho, u).  The
+// reference's E = p / ((gamma-1) rho) + Ma^2 |u|^2 / 2 only enters as rho E
+// and rho (E - Ma^2 |u|^2 / 2) + p, where the division by rho cancels: the
+// kernel forms p / (gamma-1) + rho Ma^2 |u|^2 / 2 and gamma p / (gamma-1).
+__global__ void __launch_bounds__(32 * CELLS3)
+    k3_rhs_pres(double *__restrict__ dst, SrcPtrs src, SrcPtrs gsrc, Coef3 co, int hstage,
+                Geo3 g) {
+  __shared__ double srt[CELLS3][3][NN], sut[CELLS3][3][3][NN], spt[CELLS3][3][NN];
+  __shared__ double sgr[CELLS3][4][NN], sgu[CELLS3][4][3][NN];  // gravity j < ng, kinetic
+  __shared__ double sv[CELLS3][NQ][4], sf[CELLS3][6][NF];
+  const int lc = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * CELLS3 + lc;
+  const bool active = c < g.nc;
+  const double ig = 1.0 / (GAS_GAMMA - 1.0), hgf = GAS_GAMMA / (GAS_GAMMA - 1.0);
+  const double M2 = co.Ma * co.Ma, iF2 = 1.0 / (co.Fr * co.Fr);
+  if (active) {
+    for (int j = 0; j < co.nst; ++j) {
+      tile3(srt[lc][j], src.p[3 * j], c, 1, lane);
+      tile3(&sut[lc][j][0][0], src.p[3 * j + 1], c, 3, lane);
+      tile3(spt[lc][j], src.p[3 * j + 2], c, 1, lane);
+    }
+    for (int j = 0; j <= co.ng; ++j) {  // j = ng: the kinetic (rho, u)
+      tile3(sgr[lc][j], gsrc.p[2 * j], c, 1, lane);
+      tile3(&sgu[lc][j][0][0], gsrc.p[2 * j + 1], c, 3, lane);
+    }
   }
-  double out[NN] = {0};
-  {
-    double V[NQ], Gr[NQ][3];
-    for (int q = 0; q < NQ; ++q) {
+  __syncthreads();
+  if (active) {
+    if (lane < NQ) {
+      const int q = lane;
       const double *cq = g.cg + ((long)c * NQ + q) * 13;
-      const double r0 = at_q(rt[0], q), p0 = at_q(pt[0], q);
-      double u0[3], uu0 = 0.0;
-      for (int d = 0; d < 3; ++d) { u0[d] = at_q(ut[0][d], q); uu0 += u0[d] * u0[d]; }
-      double kr, kk = 0.0;
-      {
-        double tk[NN];
-        load8(gsrc.p[2 * co.ng], c, 1, 0, tk);
-        kr = at_q(tk, q);
-        for (int d = 0; d < 3; ++d) {
-          load8(gsrc.p[2 * co.ng + 1], c, 3, d, tk);
-          const double kv = at_q(tk, q);
-          kk += kv * kv;
-        }
+      const double r0 = at_q(srt[lc][0], q), p0 = at_q(spt[lc][0], q);
+      double uu0 = 0.0;
+      for (int d = 0; d < 3; ++d) {
+        const double u = at_q(sut[lc][0][d], q);
+        uu0 += u * u;
       }
-      double v = r0 * (p0 / (gm1 * r0) + 0.5 * M2 * uu0) - 0.5 * kr * M2 * kk;
+      const double kr = at_q(sgr[lc][co.ng], q);
+      double kk = 0.0;
+      for (int d = 0; d < 3; ++d) {
+        const double kv = at_q(sgu[lc][co.ng][d], q);
+        kk += kv * kv;
+      }
+      double v = ig * p0 + 0.5 * M2 * uu0 * r0 - 0.5 * kr * M2 * kk;  // rho E - kinetic
       for (int j = 0; j < co.ng; ++j) {
-        double tk[NN];
-        load8(gsrc.p[2 * j], c, 1, 0, tk);
-        const double gr = at_q(tk, q);
+        const double gr = at_q(sgr[lc][j], q);
         double ue = 0.0;
-        for (int d = 0; d < 3; ++d) {
-          load8(gsrc.p[2 * j + 1], c, 3, d, tk);
-          ue += at_q(tk, q) * cq[10 + d];  // u . e_r a^2/r^2
-        }
+        for (int d = 0; d < 3; ++d) ue += at_q(sgu[lc][j][d], q) * cq[10 + d];  // u . e_r a^2/r^2
         v -= co.cg[j] * co.dt * M2 * iF2 * gr * ue;
       }
-      V[q] = v * cq[9];
+      sv[lc][q][0] = v * cq[9];
       double P[3] = {0, 0, 0};
       for (int j = 0; j < co.nst; ++j) {
-        const double r = at_q(rt[j], q), p = at_q(pt[j], q);
+        const double r = at_q(srt[lc][j], q), p = at_q(spt[lc][j], q);
         double u[3], uu = 0.0;
-        for (int d = 0; d < 3; ++d) { u[d] = at_q(ut[j][d], q); uu += u[d] * u[d]; }
-        const double E = p / (gm1 * r) + 0.5 * M2 * uu;
-        const double w = 0.5 * co.ca[j] * co.dt * M2 * uu * r +
-                         co.ct[j] * co.dt * (r * (E - 0.5 * M2 * uu) + p);
+        for (int d = 0; d < 3; ++d) {
+          u[d] = at_q(sut[lc][j][d], q);
+          uu += u[d] * u[d];
+        }
+        const double w = 0.5 * co.ca[j] * co.dt * M2 * uu * r + co.ct[j] * co.dt * hgf * p;
         for (int d = 0; d < 3; ++d) P[d] += w * u[d];
       }
-      to_ref(cq, P, Gr[q]);
+      to_ref(cq, P, &sv[lc][q][1]);
     }
-    integ(out, V, Gr);
-  }
-  for (int f = 0; f < 6; ++f) {
-    if (g.nbr[c * 6 + f] < 0) continue;  // no boundary term
-    double F[NF];
-    for (int q = 0; q < NF; ++q) {
-      const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
-      double uo[3][3], un[3][3];
-      for (int j = 0; j < co.nst; ++j)
-        for (int d = 0; d < 3; ++d) {
-          uo[j][d] = at_face(ut[j][d], f, q);
-          un[j][d] = nb_face(g, src.p[3 * j + 1], 3, d, c, f, q);
-        }
-      double flux = 0.0;
-      for (int j = 0; j < co.nst; ++j) {
-        const double ro = at_face(rt[j], f, q), rn = nb_face(g, src.p[3 * j], 1, 0, c, f, q);
-        const double po = at_face(pt[j], f, q), pn = nb_face(g, src.p[3 * j + 2], 1, 0, c, f, q);
-        double uuo = 0, uun = 0, uno = 0, unn = 0;
-        for (int d = 0; d < 3; ++d) {
-          uuo += uo[j][d] * uo[j][d]; uun += un[j][d] * un[j][d];
-          uno += uo[j][d] * fq[d]; unn += un[j][d] * fq[d];
-        }
-        const double akin = 0.5 * (0.5 * uuo * ro * uno + 0.5 * uun * rn * unn);
-        const double Eo = po / (gm1 * ro) + 0.5 * M2 * uuo, En = pn / (gm1 * rn) + 0.5 * M2 * uun;
-        const double ho = (Eo - 0.5 * M2 * uuo) * ro + po, hn = (En - 0.5 * M2 * uun) * rn + pn;
-        const double aent = 0.5 * (ho * uno + hn * unn);
-        const double lam = fmax(fabs(uno), fabs(unn));
-        if (hstage == 3) {
-          flux += co.ca[j] * co.dt * M2 * akin + co.ca[j] * co.dt * aent +
-                  co.ca[j] * co.dt * 0.5 * lam * (ro * Eo - rn * En);
-        } else {
-          double jk;
-          if (hstage == 2 && j == 1) {
-            double ko = 0, kn = 0;
-            for (int d = 0; d < 3; ++d) { ko += uo[1][d] * uo[0][d]; kn += un[1][d] * un[0][d]; }
-            jk = ro * 0.5 * ko - rn * 0.5 * kn;
-          } else {
-            jk = ro * 0.5 * uuo - rn * 0.5 * uun;
+    for (int e = lane; e < 6 * NF; e += 32) {
+      const int f = e / NF, q = e - f * NF;
+      double F = 0.0;
+      if (g.nbr[c * 6 + f] >= 0) {  // no boundary term
+        const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
+        double uo[3][3], un[3][3];
+        for (int j = 0; j < co.nst; ++j)
+          for (int d = 0; d < 3; ++d) {
+            uo[j][d] = at_face(sut[lc][j][d], f, q);
+            un[j][d] = nb_face(g, src.p[3 * j + 1], 3, d, c, f, q);
           }
-          const double je = ro * (Eo - 0.5 * M2 * uuo) - rn * (En - 0.5 * M2 * uun);
-          flux += co.ca[j] * co.dt * M2 * (akin + 0.5 * lam * jk) +
-                  co.ct[j] * co.dt * (aent + 0.5 * lam * je);
+        double flux = 0.0;
+        for (int j = 0; j < co.nst; ++j) {
+          const double ro = at_face(srt[lc][j], f, q), rn = nb_face(g, src.p[3 * j], 1, 0, c, f, q);
+          const double po = at_face(spt[lc][j], f, q), pn = nb_face(g, src.p[3 * j + 2], 1, 0, c, f, q);
+          double uuo = 0, uun = 0, uno = 0, unn = 0;
+          for (int d = 0; d < 3; ++d) {
+            uuo += uo[j][d] * uo[j][d]; uun += un[j][d] * un[j][d];
+            uno += uo[j][d] * fq[d]; unn += un[j][d] * fq[d];
+          }
+          const double akin = 0.5 * (0.5 * uuo * ro * uno + 0.5 * uun * rn * unn);
+          const double aent = 0.5 * (hgf * po * uno + hgf * pn * unn);
+          const double lam = fmax(fabs(uno), fabs(unn));
+          if (hstage == 3) {  // jump of the total rho E
+            const double jE = ig * (po - pn) + 0.5 * M2 * (ro * uuo - rn * uun);
+            flux += co.ca[j] * co.dt * M2 * akin + co.ca[j] * co.dt * aent +
+                    co.ca[j] * co.dt * 0.5 * lam * jE;
+          } else {
+            double jk;
+            if (hstage == 2 && j == 1) {
+              double ko = 0, kn = 0;
+              for (int d = 0; d < 3; ++d) { ko += uo[1][d] * uo[0][d]; kn += un[1][d] * un[0][d]; }
+              jk = ro * 0.5 * ko - rn * 0.5 * kn;
+            } else {
+              jk = ro * 0.5 * uuo - rn * 0.5 * uun;
+            }
+            const double je = ig * (po - pn);  // jump of rho (E - Ma^2 |u|^2 / 2)
+            flux += co.ca[j] * co.dt * M2 * (akin + 0.5 * lam * jk) +
+                    co.ct[j] * co.dt * (aent + 0.5 * lam * je);
+          }
         }
+        F = -flux * fq[3];
       }
-      F[q] = -flux * fq[3];
+      sf[lc][f][q] = F;
     }
-    for (int q = 0; q < NF; ++q)
-#pragma unroll
-      for (int i = 0; i < NN; ++i) out[i] += F[q] * c_fphi[f][q][i];
   }
-#pragma unroll
-  for (int i = 0; i < NN; ++i) dst[(long)c * NN + i] = out[i];
+  __syncthreads();
+  if (active && lane < NN) dst[(long)c * NN + lane] = gather3(sv[lc], sf[lc], lane);
 }
 
 // ------------------------------------------------------------------- B --
 // euler_operator.h:1512-1617; mode 0 dst = B p, 1 dst -= B p, 2 dst = A^{-1} B p
-__global__ void k3_B(double *__restrict__ dst, const double *__restrict__ p, double cB,
-                     const double *__restrict__ ainv, int mode, Geo3 g) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= g.nc) return;
-  double pt[NN];
-  load8(p, c, 1, 0, pt);
-  double out[3][NN] = {{0}};
-  for (int q = 0; q < NQ; ++q) {
-    const double *cq = g.cg + ((long)c * NQ + q) * 13;
-    const double s = -cB * at_q(pt, q);
-    for (int d = 0; d < 3; ++d)
+__global__ void __launch_bounds__(32 * CELLS3)
+    k3_B(double *__restrict__ dst, const double *__restrict__ p, double cB,
+         const double *__restrict__ ainv, int mode, Geo3 g) {
+  __shared__ double sp[CELLS3][NN];            // p on the cell's vertices
+  __shared__ double sgr[CELLS3][NQ][3][3];     // [q][d][e]: -cB p(q) dxi_e/dx_d JxW
+  __shared__ double sfn[CELLS3][6][NF][3];     // [f][q][d]: cB {p} n_d JxW
+  __shared__ double sout[CELLS3][3][NN];
+  const int lc = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * CELLS3 + lc;
+  const bool active = c < g.nc;
+  if (active && lane < NN) sp[lc][lane] = p[(long)c * NN + lane];
+  __syncthreads();
+  if (active) {
+    if (lane < NQ) {
+      const int q = lane;
+      const double *cq = g.cg + ((long)c * NQ + q) * 13;
+      const double s = -cB * at_q(sp[lc], q);
 #pragma unroll
-      for (int i = 0; i < NN; ++i)
-        out[d][i] += s * (cq[d] * c_dphi[q][i][0] + cq[3 + d] * c_dphi[q][i][1] +
-                          cq[6 + d] * c_dphi[q][i][2]);
-  }
-  for (int f = 0; f < 6; ++f) {
-    const bool wall = g.nbr[c * 6 + f] < 0;
-    for (int q = 0; q < NF; ++q) {
-      const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
-      const double po = at_face(pt, f, q);
-      const double pn = wall ? po : nb_face(g, p, 1, 0, c, f, q);
-      const double a = cB * 0.5 * (po + pn) * fq[3];
       for (int d = 0; d < 3; ++d)
 #pragma unroll
-        for (int i = 0; i < NN; ++i) out[d][i] += a * fq[d] * c_fphi[f][q][i];
+        for (int e = 0; e < 3; ++e) sgr[lc][q][d][e] = s * cq[3 * e + d];
+    }
+    for (int e = lane; e < 6 * NF; e += 32) {
+      const int f = e / NF, q = e - f * NF;
+      const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
+      const double po = at_face(sp[lc], f, q);
+      const double pn = g.nbr[c * 6 + f] < 0 ? po : nb_face(g, p, 1, 0, c, f, q);
+      const double a = cB * 0.5 * (po + pn) * fq[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) sfn[lc][f][q][d] = a * fq[d];
     }
   }
-  if (mode == 2) {
-    const double *A = ainv + (long)c * NN * NN;
-    for (int d = 0; d < 3; ++d)
-      for (int i = 0; i < NN; ++i) {
-        double s = 0.0;
-        for (int j = 0; j < NN; ++j) s += A[i * NN + j] * out[d][j];
-        dst[((long)c * 3 + d) * NN + i] = s;
-      }
-    return;
+  __syncthreads();
+  if (active && lane < 3 * NN) {
+    const int d = lane / NN, i = lane - d * NN;
+    double o = 0.0;
+    for (int q = 0; q < NQ; ++q)
+      o += sgr[lc][q][d][0] * c_dphi[q][i][0] + sgr[lc][q][d][1] * c_dphi[q][i][1] +
+           sgr[lc][q][d][2] * c_dphi[q][i][2];
+    for (int f = 0; f < 6; ++f)
+#pragma unroll
+      for (int q = 0; q < NF; ++q) o += sfn[lc][f][q][d] * c_fphi[f][q][i];
+    sout[lc][d][i] = o;
   }
-  for (int d = 0; d < 3; ++d)
-    for (int i = 0; i < NN; ++i) {
-      double &o = dst[((long)c * 3 + d) * NN + i];
-      o = mode == 0 ? out[d][i] : o - out[d][i];
+  __syncthreads();
+  if (active && lane < 3 * NN) {
+    const int d = lane / NN, i = lane - d * NN;
+    const long gi = ((long)c * 3 + d) * NN + i;
+    if (mode == 2) {
+      const double *A = ainv + (long)c * NN * NN + i * NN;
+      double s = 0.0;
+#pragma unroll
+      for (int j = 0; j < NN; ++j) s += A[j] * sout[lc][d][j];
+      dst[gi] = s;
+    } else {
+      dst[gi] = mode == 0 ? sout[lc][d][i] : dst[gi] - sout[lc][d][i];
     }
+  }
 }
 
 // ----------------------------------------------------------------- C/D --
 // euler_operator.h:1386-1507.  mode 0 dst = C w; 1 dst = D p - C w;
 // 2 dst = invd .* (D p - C w); 3 dst -= C w.  D = mass / (gamma - 1).
-__global__ void k3_CD(double *__restrict__ dst, const double *__restrict__ w,
-                      const double *__restrict__ p, const double *__restrict__ pfix, double cC,
-                      const double *__restrict__ invd, int mode, Geo3 g) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= g.nc) return;
+__global__ void __launch_bounds__(32 * CELLS3)
+    k3_CD(double *__restrict__ dst, const double *__restrict__ w,
+          const double *__restrict__ p, const double *__restrict__ pfix, double cC,
+          const double *__restrict__ invd, int mode, Geo3 g) {
+  __shared__ double swt[CELLS3][3][NN], sft[CELLS3][NN], spt[CELLS3][NN];
+  __shared__ double sv[CELLS3][NQ][4];         // [q]: V, Gr (3)
+  __shared__ double sfa[CELLS3][6][NF];        // [f][q]: face flux x JxW
+  const int lc = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * CELLS3 + lc;
+  const bool active = c < g.nc;
   const double hg = GAS_GAMMA / (GAS_GAMMA - 1.0);
-  double wt[3][NN], ft[NN], pt[NN];
-  for (int d = 0; d < 3; ++d) load8(w, c, 3, d, wt[d]);
-  load8(pfix, c, 1, 0, ft);
   const bool withD = mode == 1 || mode == 2;
-  if (withD) load8(p, c, 1, 0, pt);
   const double sc = withD ? -1.0 : 1.0;  // sign of C in dst
-  double out[NN] = {0};
-  double V[NQ], Gr[NQ][3];
-  for (int q = 0; q < NQ; ++q) {
-    const double *cq = g.cg + ((long)c * NQ + q) * 13;
-    const double pf = at_q(ft, q);
-    double P[3];
-    for (int d = 0; d < 3; ++d) P[d] = sc * (-cC * hg * pf * at_q(wt[d], q));
-    to_ref(cq, P, Gr[q]);
-    V[q] = withD ? at_q(pt, q) / (GAS_GAMMA - 1.0) * cq[9] : 0.0;
+  if (active && lane < 3 * NN) swt[lc][lane / NN][lane % NN] = w[(long)c * 3 * NN + lane];
+  if (active && lane < NN) {
+    sft[lc][lane] = pfix[(long)c * NN + lane];
+    if (withD) spt[lc][lane] = p[(long)c * NN + lane];
   }
-  integ(out, V, Gr);
-  for (int f = 0; f < 6; ++f) {
-    if (g.nbr[c * 6 + f] < 0) continue;  // no boundary term
-    for (int q = 0; q < NF; ++q) {
-      const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
-      const double pfo = at_face(ft, f, q), pfn = nb_face(g, pfix, 1, 0, c, f, q);
-      double av = 0.0, wno = 0.0, wnn = 0.0;
-      for (int d = 0; d < 3; ++d) {
-        const double wo = at_face(wt[d], f, q), wn = nb_face(g, w, 3, d, c, f, q);
-        av += 0.5 * hg * (pfo * wo + pfn * wn) * fq[d];
-        wno += wo * fq[d];
-        wnn += wn * fq[d];
-      }
-      const double lam = fmax(fabs(wno), fabs(wnn));
-      const double a = sc * cC * (av + 0.5 * lam * (pfo - pfn) / (GAS_GAMMA - 1.0)) * fq[3];
+  __syncthreads();
+  if (active) {
+    if (lane < NQ) {
+      const int q = lane;
+      const double *cq = g.cg + ((long)c * NQ + q) * 13;
+      const double pf = at_q(sft[lc], q);
+      double P[3];
 #pragma unroll
-      for (int i = 0; i < NN; ++i) out[i] += a * c_fphi[f][q][i];
+      for (int d = 0; d < 3; ++d) P[d] = sc * (-cC * hg * pf * at_q(swt[lc][d], q));
+      double Gr[3];
+      to_ref(cq, P, Gr);
+      sv[lc][q][0] = withD ? at_q(spt[lc], q) / (GAS_GAMMA - 1.0) * cq[9] : 0.0;
+#pragma unroll
+      for (int e = 0; e < 3; ++e) sv[lc][q][1 + e] = Gr[e];
+    }
+    for (int e = lane; e < 6 * NF; e += 32) {
+      const int f = e / NF, q = e - f * NF;
+      double a = 0.0;
+      if (g.nbr[c * 6 + f] >= 0) {  // no boundary term
+        const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
+        const double pfo = at_face(sft[lc], f, q), pfn = nb_face(g, pfix, 1, 0, c, f, q);
+        double av = 0.0, wno = 0.0, wnn = 0.0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const double wo = at_face(swt[lc][d], f, q), wn = nb_face(g, w, 3, d, c, f, q);
+          av += 0.5 * hg * (pfo * wo + pfn * wn) * fq[d];
+          wno += wo * fq[d];
+          wnn += wn * fq[d];
+        }
+        const double lam = fmax(fabs(wno), fabs(wnn));
+        a = sc * cC * (av + 0.5 * lam * (pfo - pfn) / (GAS_GAMMA - 1.0)) * fq[3];
+      }
+      sfa[lc][f][q] = a;
     }
   }
-  for (int i = 0; i < NN; ++i) {
+  __syncthreads();
+  if (active && lane < NN) {
+    const int i = lane;
+    double o = 0.0;
+    for (int q = 0; q < NQ; ++q)
+      o += sv[lc][q][0] * c_phi[q][i] + sv[lc][q][1] * c_dphi[q][i][0] +
+           sv[lc][q][2] * c_dphi[q][i][1] + sv[lc][q][3] * c_dphi[q][i][2];
+    for (int f = 0; f < 6; ++f)
+#pragma unroll
+      for (int q = 0; q < NF; ++q) o += sfa[lc][f][q] * c_fphi[f][q][i];
     const long gi = (long)c * NN + i;
-    if (mode == 2) dst[gi] = invd[gi] * out[i];
-    else if (mode == 3) dst[gi] -= out[i];
-    else dst[gi] = out[i];
+    if (mode == 2) dst[gi] = invd[gi] * o;
+    else if (mode == 3) dst[gi] -= o;
+    else dst[gi] = o;
   }
 }
 
@@ -688,7 +764,7 @@ int rhs_rho3(atm3_ctx &c, double *dst, const double *const *src) {
   SrcPtrs sp{};
   const Coef3 co = coef3(c, c.hstage, true);
   for (int i = 0; i < 2 * co.nst; ++i) sp.p[i] = src[i];
-  k3_rhs_rho<<<blocks(c.nc), 128, 0, c.stream>>>(dst, sp, co, c.g);
+  k3_rhs_rho<<<(c.nc + CELLS3 - 1) / CELLS3, 32 * CELLS3, 0, c.stream>>>(dst, sp, co, c.g);
   ATM_CHECK_LAUNCH("k3_rhs_rho");
   return ATM_OK;
 }
@@ -701,7 +777,7 @@ int rhs_vel3(atm3_ctx &c, double *dst, const double *const *src) {
   gp.p[0] = src[0];
   gp.p[1] = src[3];
   if (co.ng > 2) gp.p[2] = src[6];
-  k3_rhs_vel<<<blocks(c.nc), 128, 0, c.stream>>>(dst, sp, gp, co, c.g);
+  k3_rhs_vel<<<(c.nc + CELLS3 - 1) / CELLS3, 32 * CELLS3, 0, c.stream>>>(dst, sp, gp, co, c.g);
   ATM_CHECK_LAUNCH("k3_rhs_vel");
   return ATM_OK;
 }
@@ -721,17 +797,18 @@ int rhs_pres3(atm3_ctx &c, double *dst, const double *const *src) {
     const double *g[] = {src[0], src[1], src[3], src[4], src[6], src[7], src[9], src[10]};
     for (int i = 0; i < 8; ++i) gp.p[i] = g[i];
   }
-  k3_rhs_pres<<<blocks(c.nc), 128, 0, c.stream>>>(dst, sp, gp, co, c.hstage, c.g);
+  k3_rhs_pres<<<(c.nc + CELLS3 - 1) / CELLS3, 32 * CELLS3, 0, c.stream>>>(dst, sp, gp, co, c.hstage, c.g);
   ATM_CHECK_LAUNCH("k3_rhs_pres");
   return ATM_OK;
 }
 int B3(atm3_ctx &c, double *dst, const double *p, double cB, int mode) {
-  k3_B<<<blocks(c.nc), 128, 0, c.stream>>>(dst, p, cB, c.ainv, mode, c.g);
+  k3_B<<<(c.nc + CELLS3 - 1) / CELLS3, 32 * CELLS3, 0, c.stream>>>(dst, p, cB, c.ainv, mode, c.g);
   ATM_CHECK_LAUNCH("k3_B");
   return ATM_OK;
 }
 int CD3(atm3_ctx &c, double *dst, const double *w, const double *p, double cC, int mode) {
-  k3_CD<<<blocks(c.nc), 128, 0, c.stream>>>(dst, w, p, c.pres_fix, cC, c.invd, mode, c.g);
+  k3_CD<<<(c.nc + CELLS3 - 1) / CELLS3, 32 * CELLS3, 0, c.stream>>>(dst, w, p, c.pres_fix, cC, c.invd,
+                                                                      mode, c.g);
   ATM_CHECK_LAUNCH("k3_CD");
   return ATM_OK;
 }
