@@ -220,6 +220,19 @@ int vec_scale_by_inv_norm(cudaStream_t st, double *dst, const double *src,
 constexpr int RED_BLOCKS = 608;
 int vec_dot(cudaStream_t st, const double *x, const double *y, long n, double *red,
             double *out);  // out[0] = x.y (device)
+// One Arnoldi orthogonalisation of the new direction w against V_0..V_j,
+// all of length n with stride n: classical Gram-Schmidt with one
+// re-orthogonalisation pass (CGS2), then V_{j+1} = w / |w| when |w| is
+// nonzero (w is overwritten by the unscaled result).  hcol[0..j] gets the projection
+// coefficients, *hn the remaining norm.  `dsmall` is device scratch of >= 65
+// values (dsmall[64] ends as |V_{j+1}|^2 before the scaling), `h_pinned` a
+// pinned host mirror of >= 65; one stream synchronisation.  (A second pass
+// only when the first cancels, by the criterion of Daniel, Gragg, Kaufman
+// and Stewart, saves nothing here: with the Jacobi-scaled Schur operator
+// close to the identity the first pass always cancels, and the extra
+// synchronisation made the step slower.)
+int arnoldi_step(cudaStream_t st, double *V, long n, int j, double *w, double *red,
+                 double *dsmall, double *h_pinned, double *hcol, double *hn);
 int vec_multidot(cudaStream_t st, const double *V, long ldv, int m, const double *w, long n,
                  double *red, double *out);  // out[l] = V_l . w, l < m
 // w += sign * sum_l h[l] V_l  (h device)

@@ -5,6 +5,7 @@
 // They replace the deal.II vector operations used by SolverCG/SolverGMRES and
 // the diagnostics of Atmospheric_Flow.cc:991-1087, 1140-1148.
 #include <cfloat>
+#include <cmath>
 
 #include "atm_device.cuh"
 
@@ -254,6 +255,23 @@ int vec_multiaxpy(cudaStream_t st, double *w, const double *V, long ldv, int m,
   if (m < 1) return ATM_OK;
   k_multiaxpy<<<grid_for(n), 256, 0, st>>>(w, V, ldv, m, h, sign, n);
   ATM_CHECK_LAUNCH("k_multiaxpy");
+  return ATM_OK;
+}
+int arnoldi_step(cudaStream_t st, double *V, long n, int j, double *w, double *red,
+                 double *dsmall, double *h_pinned, double *hcol, double *hn) {
+  double *h1 = dsmall, *h2 = dsmall + 32, *nsq = dsmall + 64;
+  int rc;
+  if ((rc = vec_multidot(st, V, n, j + 1, w, n, red, h1))) return rc;
+  if ((rc = vec_multiaxpy(st, w, V, n, j + 1, h1, -1.0, n))) return rc;
+  if ((rc = vec_multidot(st, V, n, j + 1, w, n, red, h2))) return rc;
+  if ((rc = vec_multiaxpy(st, w, V, n, j + 1, h2, -1.0, n))) return rc;
+  if ((rc = vec_dot(st, w, w, n, red, nsq))) return rc;
+  ATM_CUDA(cudaMemcpyAsync(h_pinned, dsmall, 65 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  ATM_CUDA(cudaStreamSynchronize(st));
+  for (int l = 0; l <= j; ++l) hcol[l] = h_pinned[l] + h_pinned[32 + l];
+  *hn = std::sqrt(h_pinned[64]);
+  if (*hn > 0.0 && std::isfinite(*hn))
+    if ((rc = vec_scale_by_inv_norm(st, V + (long)(j + 1) * n, w, nsq, n))) return rc;
   return ATM_OK;
 }
 int vec_maxdiff(cudaStream_t st, const double *a, const double *b, long n, double *red,

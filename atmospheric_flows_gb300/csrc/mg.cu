@@ -816,8 +816,8 @@ int mg_precondition(atm_ctx &c, int precision, double *z, const double *v) {
 
 // FGMRES(m) on S x = b with the V-cycle as right preconditioner; stops when
 // the (unpreconditioned) residual estimate <= tol, or, with the true-residual
-// check on, when the recomputed residual is.  Same CGS2 / Givens machinery
-// as gmres_schur.
+// check on, when the recomputed residual is.  Same CGS2 (arnoldi_step) and
+// Givens machinery as gmres_schur.
 int fgmres_mg(atm_ctx &c, int precision, double *x, const double *b, double tol, int maxit,
               int *its, double *res) {
   if (!c.mg || c.mg->hm.size() < 2) {
@@ -835,8 +835,8 @@ int fgmres_mg(atm_ctx &c, int precision, double *x, const double *b, double tol,
   const int m = mg.restart;
   double *V = c.krylov, *Z = mg.zbasis;
   double *w = c.ws1, *t = c.ws2;
-  double *h1 = c.dsmall, *h2 = c.dsmall + 32, *nsq = c.dsmall + 64, *ydev = c.dsmall + 96;
-  std::vector<double> H((m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m);
+  double *nsq = c.dsmall + 64, *ydev = c.dsmall + 96;
+  std::vector<double> H((m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m), hcol(m + 1);
   *its = 0;
   *res = 0.0;
   for (;;) {
@@ -862,16 +862,10 @@ int fgmres_mg(atm_ctx &c, int precision, double *x, const double *b, double tol,
                           : precondition<float>(c, mg, Z + (long)j * n, V + (long)j * n);
       if (rc) return rc;
       if ((rc = schur_apply(c, w, Z + (long)j * n, false))) return rc;
-      if ((rc = vec_multidot(c.stream, V, n, j + 1, w, n, c.red, h1))) return rc;
-      if ((rc = vec_multiaxpy(c.stream, w, V, n, j + 1, h1, -1.0, n))) return rc;
-      if ((rc = vec_multidot(c.stream, V, n, j + 1, w, n, c.red, h2))) return rc;
-      if ((rc = vec_multiaxpy(c.stream, w, V, n, j + 1, h2, -1.0, n))) return rc;
-      if ((rc = vec_dot(c.stream, w, w, n, c.red, nsq))) return rc;
-      ATM_CUDA(cudaMemcpyAsync(c.h_red, c.dsmall, 65 * sizeof(double), cudaMemcpyDeviceToHost,
-                               c.stream));
-      ATM_CUDA(cudaStreamSynchronize(c.stream));
-      for (int l = 0; l <= j; ++l) H[l * m + j] = c.h_red[l] + c.h_red[32 + l];
-      const double hn = std::sqrt(c.h_red[64]);
+      double hn = 0.0;
+      if ((rc = arnoldi_step(c.stream, V, n, j, w, c.red, c.dsmall, c.h_red, hcol.data(), &hn)))
+        return rc;
+      for (int l = 0; l <= j; ++l) H[l * m + j] = hcol[l];
       if (!std::isfinite(hn)) { set_error("FGMRES: non-finite Arnoldi vector"); return ATM_NONFINITE; }
       H[(j + 1) * m + j] = hn;
       for (int l = 0; l < j; ++l) {
@@ -889,8 +883,6 @@ int fgmres_mg(atm_ctx &c, int precision, double *x, const double *b, double tol,
       g[j] = cs[j] * g[j];
       jend = j + 1;
       *res = std::fabs(g[j + 1]);
-      if (hn > 0.0)
-        if ((rc = vec_scale_by_inv_norm(c.stream, V + (long)(j + 1) * n, w, nsq, n))) return rc;
       if (*res <= tol || hn == 0.0 || *its >= maxit) { done = true; break; }
     }
     for (int l = jend - 1; l >= 0; --l) {

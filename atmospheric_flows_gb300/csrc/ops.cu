@@ -117,16 +117,16 @@ int op_solve(atm_ctx &c, double *x, const double *b, double tol, int maxit, int 
 
 // Restarted GMRES with left Jacobi preconditioning (deal.II SolverGMRES with
 // right_preconditioning = false, max_n_tmp_vectors = 30 -> 28 basis vectors):
-// classical Gram-Schmidt with one re-orthogonalisation pass (CGS2), Givens
-// rotations, stop when the preconditioned residual estimate <= tol.
-// The same algorithm is restated in the CPU oracle.
+// classical Gram-Schmidt with one re-orthogonalisation pass (CGS2,
+// arnoldi_step), Givens rotations, stop when the preconditioned residual
+// estimate <= tol.  The same algorithm is restated in the CPU oracle.
 int gmres_schur(atm_ctx &c, double *x, const double *b, double tol, int maxit, int *its,
                 double *res) {
   const long n = c.n_scalar();
   const int m = c.restart;
   double *V = c.krylov;
   double *w = c.ws1, *t = c.ws2;
-  double *h1 = c.dsmall, *h2 = c.dsmall + 32, *nsq = c.dsmall + 64, *ydev = c.dsmall + 96;
+  double *nsq = c.dsmall + 64, *ydev = c.dsmall + 96;
   std::vector<double> H((m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m), hcol(m + 1);
   int rc;
   *its = 0;
@@ -150,14 +150,10 @@ int gmres_schur(atm_ctx &c, double *x, const double *b, double tol, int maxit, i
       ++*its;
       double *Vj = V + (long)j * n;
       if ((rc = schur_apply(c, w, Vj, true))) return rc;
-      if ((rc = vec_multidot(c.stream, V, n, j + 1, w, n, c.red, h1))) return rc;
-      if ((rc = vec_multiaxpy(c.stream, w, V, n, j + 1, h1, -1.0, n))) return rc;
-      if ((rc = vec_multidot(c.stream, V, n, j + 1, w, n, c.red, h2))) return rc;
-      if ((rc = vec_multiaxpy(c.stream, w, V, n, j + 1, h2, -1.0, n))) return rc;
-      if ((rc = vec_dot(c.stream, w, w, n, c.red, nsq))) return rc;
-      if ((rc = read_small(c, c.dsmall, 65))) return rc;
-      for (int l = 0; l <= j; ++l) H[l * m + j] = c.h_red[l] + c.h_red[32 + l];
-      const double hn = std::sqrt(c.h_red[64]);
+      double hn = 0.0;
+      if ((rc = arnoldi_step(c.stream, V, n, j, w, c.red, c.dsmall, c.h_red, hcol.data(), &hn)))
+        return rc;
+      for (int l = 0; l <= j; ++l) H[l * m + j] = hcol[l];
       if (!std::isfinite(hn)) { set_error("GMRES: non-finite Arnoldi vector"); return ATM_NONFINITE; }
       H[(j + 1) * m + j] = hn;
       for (int l = 0; l < j; ++l) {
@@ -175,8 +171,6 @@ int gmres_schur(atm_ctx &c, double *x, const double *b, double tol, int maxit, i
       g[j] = cs[j] * g[j];
       jend = j + 1;
       *res = std::fabs(g[j + 1]);
-      if (hn > 0.0)
-        if ((rc = vec_scale_by_inv_norm(c.stream, V + (long)(j + 1) * n, w, nsq, n))) return rc;
       if (*res <= tol || hn == 0.0 || *its >= maxit) { done = true; break; }
     }
     for (int l = jend - 1; l >= 0; --l) {

@@ -845,14 +845,14 @@ int vmult3(atm3_ctx &c, double *dst, const double *src) {
   return ATM_OK;
 }
 
-// GMRES(28) + left Jacobi on diag(D), CGS2, Givens; the algorithm of the 2D
-// path's gmres_schur on the 3D operator
+// GMRES(28) + left Jacobi on diag(D), CGS2 (arnoldi_step), Givens; the
+// algorithm of the 2D path's gmres_schur on the 3D operator
 int gmres3(atm3_ctx &c, double *x, const double *b, double tol, int maxit, int *its, double *res) {
   const long n = c.ns();
   const int m = RESTART3;
   double *V = c.krylov, *w = c.ws1, *t = c.ws2;
-  double *h1 = c.dsmall, *h2 = c.dsmall + 32, *nsq = c.dsmall + 64, *ydev = c.dsmall + 96;
-  std::vector<double> H((m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m);
+  double *nsq = c.dsmall + 64, *ydev = c.dsmall + 96;
+  std::vector<double> H((m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m), hcol(m + 1);
   *its = 0;
   *res = 0.0;
   for (;;) {
@@ -873,14 +873,9 @@ int gmres3(atm3_ctx &c, double *x, const double *b, double tol, int maxit, int *
     for (int j = 0; j < m; ++j) {
       ++*its;
       TRY3(schur3(c, w, V + (long)j * n, true));
-      TRY3(vec_multidot(c.stream, V, n, j + 1, w, n, c.red, h1));
-      TRY3(vec_multiaxpy(c.stream, w, V, n, j + 1, h1, -1.0, n));
-      TRY3(vec_multidot(c.stream, V, n, j + 1, w, n, c.red, h2));
-      TRY3(vec_multiaxpy(c.stream, w, V, n, j + 1, h2, -1.0, n));
-      TRY3(vec_dot(c.stream, w, w, n, c.red, nsq));
-      TRY3(read3(c, c.dsmall, 65));
-      for (int l = 0; l <= j; ++l) H[l * m + j] = c.h_red[l] + c.h_red[32 + l];
-      const double hn = std::sqrt(c.h_red[64]);
+      double hn = 0.0;
+      TRY3(arnoldi_step(c.stream, V, n, j, w, c.red, c.dsmall, c.h_red, hcol.data(), &hn));
+      for (int l = 0; l <= j; ++l) H[l * m + j] = hcol[l];
       if (!std::isfinite(hn)) { set_error("GMRES: non-finite Arnoldi vector"); return ATM_NONFINITE; }
       H[(j + 1) * m + j] = hn;
       for (int l = 0; l < j; ++l) {
@@ -898,7 +893,6 @@ int gmres3(atm3_ctx &c, double *x, const double *b, double tol, int maxit, int *
       g[j] = cs[j] * g[j];
       jend = j + 1;
       *res = std::fabs(g[j + 1]);
-      if (hn > 0.0) TRY3(vec_scale_by_inv_norm(c.stream, V + (long)(j + 1) * n, w, nsq, n));
       if (*res <= tol || hn == 0.0 || *its >= maxit) { done = true; break; }
     }
     for (int l = jend - 1; l >= 0; --l) {
