@@ -60,21 +60,33 @@ __device__ __forceinline__ double at_q(const double *t, int q) {
   for (int i = 0; i < NN; ++i) s = fma(c_phi[q][i], t[i], s);
   return s;
 }
+// k-th (k < 4) vertex of local face f, in increasing vertex order: the
+// vertices whose bit f/2 equals f%2.  The other four basis functions vanish
+// on the face exactly, so the face sums below skip them.
+__device__ __forceinline__ int fnode(int f, int k) {
+  const int a = f >> 1, lo = k & ((1 << a) - 1);
+  return lo | ((f & 1) << a) | ((k >> a) << (a + 1));
+}
 __device__ __forceinline__ double at_face(const double *t, int f, int q) {
   double s = 0.0;
 #pragma unroll
-  for (int i = 0; i < NN; ++i) s = fma(c_fphi[f][q][i], t[i], s);
+  for (int k = 0; k < 4; ++k) s = fma(c_fphi[f][q][fnode(f, k)], t[fnode(f, k)], s);
   return s;
 }
-// neighbour's trace matching own face point q of face f (nb >= 0)
-__device__ __forceinline__ double nb_face(const Geo3 &g, const double *v, int ncomp, int comp,
-                                          int c, int f, int q) {
-  const int nb = g.nbr[c * 6 + f], nf = g.nbf[c * 6 + f];
-  const int qn = g.nperm[(c * 6 + f) * NF + q];
-  const double *s = v + ((long)nb * ncomp + comp) * NN;
+// the neighbour across face f of cell c at own face point q: its cell, its
+// local face and the matching point there (loaded once per face point)
+struct NbPt {
+  int nb, nf, qn;
+};
+__device__ __forceinline__ NbPt nb_point(const Geo3 &g, int c, int f, int q) {
+  return NbPt{g.nbr[c * 6 + f], g.nbf[c * 6 + f], g.nperm[(c * 6 + f) * NF + q]};
+}
+// the neighbour's trace of component comp of a field with ncomp components
+__device__ __forceinline__ double nb_val(const NbPt &n, const double *v, int ncomp, int comp) {
+  const double *s = v + ((long)n.nb * ncomp + comp) * NN;
   double r = 0.0;
 #pragma unroll
-  for (int i = 0; i < NN; ++i) r = fma(c_fphi[nf][qn][i], s[i], r);
+  for (int k = 0; k < 4; ++k) r = fma(c_fphi[n.nf][n.qn][fnode(n.nf, k)], s[fnode(n.nf, k)], r);
   return r;
 }
 // out[i] += sum_q (V_q phi_i + sum_e Gr_q[e] dphi_i/dxi_e) at the cell points;
@@ -115,9 +127,11 @@ __device__ __forceinline__ double gather3(const double (*sv)[4], const double (*
   for (int q = 0; q < NQ; ++q)
     o += sv[q][0] * c_phi[q][i] + sv[q][1] * c_dphi[q][i][0] + sv[q][2] * c_dphi[q][i][1] +
          sv[q][3] * c_dphi[q][i][2];
-  for (int f = 0; f < 6; ++f)
+  for (int a = 0; a < 3; ++a) {  // the faces holding vertex i, in increasing order
+    const int f = 2 * a + ((i >> a) & 1);
 #pragma unroll
     for (int q = 0; q < NF; ++q) o += sf[f][q] * c_fphi[f][q][i];
+  }
   return o;
 }
 
@@ -154,12 +168,13 @@ __global__ void __launch_bounds__(32 * CELLS3)
       if (g.nbr[c * 6 + f] >= 0) {  // no boundary term (euler_operator.h:111-114)
         const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
         double flux = 0.0;
+        const NbPt np = nb_point(g, c, f, q);
         for (int j = 0; j < co.nst; ++j) {
-          const double ro = at_face(srt[lc][j], f, q), rn = nb_face(g, src.p[2 * j], 1, 0, c, f, q);
+          const double ro = at_face(srt[lc][j], f, q), rn = nb_val(np, src.p[2 * j], 1, 0);
           double avg = 0.0, uno = 0.0, unn = 0.0;
           for (int d = 0; d < 3; ++d) {
             const double uo = at_face(sut[lc][j][d], f, q);
-            const double un = nb_face(g, src.p[2 * j + 1], 3, d, c, f, q);
+            const double un = nb_val(np, src.p[2 * j + 1], 3, d);
             avg += 0.5 * (ro * uo + rn * un) * fq[d];
             uno += uo * fq[d];
             unn += un * fq[d];
@@ -216,7 +231,8 @@ __global__ void __launch_bounds__(32 * CELLS3)
     }
     for (int e = lane; e < 6 * NF; e += 32) {
       const int f = e / NF, q = e - f * NF;
-      const bool wall = g.nbr[c * 6 + f] < 0;
+      const NbPt np = nb_point(g, c, f, q);
+      const bool wall = np.nb < 0;
       const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
       double fl[3] = {0, 0, 0};
       for (int j = 0; j < co.nst; ++j) {
@@ -225,12 +241,12 @@ __global__ void __launch_bounds__(32 * CELLS3)
           for (int d = 0; d < 3; ++d) fl[d] += co.ct[j] * co.dt * iM2 * 0.5 * (po + po) * fq[d];
           continue;
         }
-        const double ro = at_face(srt[lc][j], f, q), rn = nb_face(g, src.p[3 * j], 1, 0, c, f, q);
-        const double pn = nb_face(g, src.p[3 * j + 2], 1, 0, c, f, q);
+        const double ro = at_face(srt[lc][j], f, q), rn = nb_val(np, src.p[3 * j], 1, 0);
+        const double pn = nb_val(np, src.p[3 * j + 2], 1, 0);
         double uo[3], un[3], uno = 0.0, unn = 0.0;
         for (int k = 0; k < 3; ++k) {
           uo[k] = at_face(sut[lc][j][k], f, q);
-          un[k] = nb_face(g, src.p[3 * j + 1], 3, k, c, f, q);
+          un[k] = nb_val(np, src.p[3 * j + 1], 3, k);
           uno += uo[k] * fq[k];
           unn += un[k] * fq[k];
         }
@@ -323,16 +339,17 @@ __global__ void __launch_bounds__(32 * CELLS3)
       double F = 0.0;
       if (g.nbr[c * 6 + f] >= 0) {  // no boundary term
         const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
+        const NbPt np = nb_point(g, c, f, q);
         double uo[3][3], un[3][3];
         for (int j = 0; j < co.nst; ++j)
           for (int d = 0; d < 3; ++d) {
             uo[j][d] = at_face(sut[lc][j][d], f, q);
-            un[j][d] = nb_face(g, src.p[3 * j + 1], 3, d, c, f, q);
+            un[j][d] = nb_val(np, src.p[3 * j + 1], 3, d);
           }
         double flux = 0.0;
         for (int j = 0; j < co.nst; ++j) {
-          const double ro = at_face(srt[lc][j], f, q), rn = nb_face(g, src.p[3 * j], 1, 0, c, f, q);
-          const double po = at_face(spt[lc][j], f, q), pn = nb_face(g, src.p[3 * j + 2], 1, 0, c, f, q);
+          const double ro = at_face(srt[lc][j], f, q), rn = nb_val(np, src.p[3 * j], 1, 0);
+          const double po = at_face(spt[lc][j], f, q), pn = nb_val(np, src.p[3 * j + 2], 1, 0);
           double uuo = 0, uun = 0, uno = 0, unn = 0;
           for (int d = 0; d < 3; ++d) {
             uuo += uo[j][d] * uo[j][d]; uun += un[j][d] * un[j][d];
@@ -396,7 +413,8 @@ __global__ void __launch_bounds__(32 * CELLS3)
       const int f = e / NF, q = e - f * NF;
       const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
       const double po = at_face(sp[lc], f, q);
-      const double pn = g.nbr[c * 6 + f] < 0 ? po : nb_face(g, p, 1, 0, c, f, q);
+      const NbPt np = nb_point(g, c, f, q);
+      const double pn = np.nb < 0 ? po : nb_val(np, p, 1, 0);
       const double a = cB * 0.5 * (po + pn) * fq[3];
 #pragma unroll
       for (int d = 0; d < 3; ++d) sfn[lc][f][q][d] = a * fq[d];
@@ -409,9 +427,11 @@ __global__ void __launch_bounds__(32 * CELLS3)
     for (int q = 0; q < NQ; ++q)
       o += sgr[lc][q][d][0] * c_dphi[q][i][0] + sgr[lc][q][d][1] * c_dphi[q][i][1] +
            sgr[lc][q][d][2] * c_dphi[q][i][2];
-    for (int f = 0; f < 6; ++f)
+    for (int a = 0; a < 3; ++a) {  // the faces holding vertex i
+      const int f = 2 * a + ((i >> a) & 1);
 #pragma unroll
       for (int q = 0; q < NF; ++q) o += sfn[lc][f][q][d] * c_fphi[f][q][i];
+    }
     sout[lc][d][i] = o;
   }
   __syncthreads();
@@ -469,13 +489,14 @@ __global__ void __launch_bounds__(32 * CELLS3)
     for (int e = lane; e < 6 * NF; e += 32) {
       const int f = e / NF, q = e - f * NF;
       double a = 0.0;
-      if (g.nbr[c * 6 + f] >= 0) {  // no boundary term
+      const NbPt np = nb_point(g, c, f, q);
+      if (np.nb >= 0) {  // no boundary term
         const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
-        const double pfo = at_face(sft[lc], f, q), pfn = nb_face(g, pfix, 1, 0, c, f, q);
+        const double pfo = at_face(sft[lc], f, q), pfn = nb_val(np, pfix, 1, 0);
         double av = 0.0, wno = 0.0, wnn = 0.0;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-          const double wo = at_face(swt[lc][d], f, q), wn = nb_face(g, w, 3, d, c, f, q);
+          const double wo = at_face(swt[lc][d], f, q), wn = nb_val(np, w, 3, d);
           av += 0.5 * hg * (pfo * wo + pfn * wn) * fq[d];
           wno += wo * fq[d];
           wnn += wn * fq[d];
