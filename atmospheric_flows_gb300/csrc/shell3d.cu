@@ -120,9 +120,33 @@ __device__ __forceinline__ void tile3(double *dst, const double *src, int c, int
   for (int e = lane; e < ncomp * NN; e += 32) dst[e] = src[(long)c * ncomp * NN + e];
 }
 
-// sum over the cell's points of V_q phi_i + Gr_q . grad phi_i, then over the
-// face points of F_fq phi_i (the order of the one-thread version)
-__device__ __forceinline__ double gather3(const double (*sv)[4], const double (*sf)[NF], int i) {
+// For vertex i = lane % 8: the sum over the cell's points of
+// V_q phi_i + Gr_q . grad phi_i and over the points of the three faces that
+// hold the vertex of F_fq phi_i.  The four lanes of each vertex take every
+// fourth term and the partial sums are combined by shuffles, so that all 32
+// lanes work (an FP64 warp instruction costs the same with 8 active lanes as
+// with 32).  Every lane of the warp must call it; lanes 0..7 hold the result
+// of their vertex (all lanes do).
+__device__ __forceinline__ double gather3(const double (*sv)[4], const double (*sf)[NF],
+                                          int lane) {
+  const int i = lane & 7, part = lane >> 3;
+  double o = 0.0;
+  for (int q = part; q < NQ; q += 4)
+    o += sv[q][0] * c_phi[q][i] + sv[q][1] * c_dphi[q][i][0] + sv[q][2] * c_dphi[q][i][1] +
+         sv[q][3] * c_dphi[q][i][2];
+  for (int t = part; t < 3 * NF; t += 4) {
+    const int a = t / NF, q = t - a * NF, f = 2 * a + ((i >> a) & 1);
+    o += sf[f][q] * c_fphi[f][q][i];
+  }
+  o += __shfl_xor_sync(0xffffffffu, o, 8);
+  o += __shfl_xor_sync(0xffffffffu, o, 16);
+  return o;
+}
+
+// The same sums for vertex i by one lane alone (three components at once
+// keep 24 of the 32 lanes busy without the shuffles)
+__device__ __forceinline__ double gather3_one(const double (*sv)[4], const double (*sf)[NF],
+                                              int i) {
   double o = 0.0;
   for (int q = 0; q < NQ; ++q)
     o += sv[q][0] * c_phi[q][i] + sv[q][1] * c_dphi[q][i][0] + sv[q][2] * c_dphi[q][i][1] +
@@ -187,7 +211,10 @@ __global__ void __launch_bounds__(32 * CELLS3)
     }
   }
   __syncthreads();
-  if (active && lane < NN) dst[(long)c * NN + lane] = gather3(sv[lc], sf[lc], lane);
+  if (active) {  // warp-uniform: every lane of the cell's warp takes part
+    const double o = gather3(sv[lc], sf[lc], lane);
+    if (lane < NN) dst[(long)c * NN + lane] = o;
+  }
 }
 
 // ------------------------------------------------------------ momentum --
@@ -262,7 +289,7 @@ __global__ void __launch_bounds__(32 * CELLS3)
   __syncthreads();
   if (active && lane < 3 * NN) {
     const int d = lane / NN, i = lane - d * NN;
-    dst[((long)c * 3 + d) * NN + i] = gather3(sv[lc][d], sf[lc][d], i);
+    dst[((long)c * 3 + d) * NN + i] = gather3_one(sv[lc][d], sf[lc][d], i);
   }
 }
 
@@ -382,7 +409,10 @@ __global__ void __launch_bounds__(32 * CELLS3)
     }
   }
   __syncthreads();
-  if (active && lane < NN) dst[(long)c * NN + lane] = gather3(sv[lc], sf[lc], lane);
+  if (active) {  // warp-uniform: every lane of the cell's warp takes part
+    const double o = gather3(sv[lc], sf[lc], lane);
+    if (lane < NN) dst[(long)c * NN + lane] = o;
+  }
 }
 
 // ------------------------------------------------------------------- B --
@@ -463,7 +493,9 @@ __global__ void __launch_bounds__(32 * CELLS3)
   const int lc = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = blockIdx.x * CELLS3 + lc;
   const bool active = c < g.nc;
-  const double hg = GAS_GAMMA / (GAS_GAMMA - 1.0);
+  // 1/(gamma-1) as a constant factor: a division by (gamma-1) at every point
+  // would cost an FP64 division sequence each (the values agree to rounding)
+  const double hg = GAS_GAMMA / (GAS_GAMMA - 1.0), ig = 1.0 / (GAS_GAMMA - 1.0);
   const bool withD = mode == 1 || mode == 2;
   const double sc = withD ? -1.0 : 1.0;  // sign of C in dst
   if (active && lane < 3 * NN) swt[lc][lane / NN][lane % NN] = w[(long)c * 3 * NN + lane];
@@ -482,7 +514,7 @@ __global__ void __launch_bounds__(32 * CELLS3)
       for (int d = 0; d < 3; ++d) P[d] = sc * (-cC * hg * pf * at_q(swt[lc][d], q));
       double Gr[3];
       to_ref(cq, P, Gr);
-      sv[lc][q][0] = withD ? at_q(spt[lc], q) / (GAS_GAMMA - 1.0) * cq[9] : 0.0;
+      sv[lc][q][0] = withD ? at_q(spt[lc], q) * ig * cq[9] : 0.0;
 #pragma unroll
       for (int e = 0; e < 3; ++e) sv[lc][q][1 + e] = Gr[e];
     }
@@ -502,21 +534,16 @@ __global__ void __launch_bounds__(32 * CELLS3)
           wnn += wn * fq[d];
         }
         const double lam = fmax(fabs(wno), fabs(wnn));
-        a = sc * cC * (av + 0.5 * lam * (pfo - pfn) / (GAS_GAMMA - 1.0)) * fq[3];
+        a = sc * cC * (av + 0.5 * lam * (pfo - pfn) * ig) * fq[3];
       }
       sfa[lc][f][q] = a;
     }
   }
   __syncthreads();
-  if (active && lane < NN) {
+  if (active) {  // warp-uniform: every lane of the cell's warp takes part
+    const double o = gather3(sv[lc], sfa[lc], lane);
+    if (lane >= NN) return;
     const int i = lane;
-    double o = 0.0;
-    for (int q = 0; q < NQ; ++q)
-      o += sv[lc][q][0] * c_phi[q][i] + sv[lc][q][1] * c_dphi[q][i][0] +
-           sv[lc][q][2] * c_dphi[q][i][1] + sv[lc][q][3] * c_dphi[q][i][2];
-    for (int f = 0; f < 6; ++f)
-#pragma unroll
-      for (int q = 0; q < NF; ++q) o += sfa[lc][f][q] * c_fphi[f][q][i];
     const long gi = (long)c * NN + i;
     if (mode == 2) dst[gi] = invd[gi] * o;
     else if (mode == 3) dst[gi] -= o;
