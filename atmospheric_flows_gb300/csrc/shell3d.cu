@@ -89,6 +89,49 @@ __device__ __forceinline__ double nb_val(const NbPt &n, const double *v, int nco
   for (int k = 0; k < 4; ++k) r = fma(c_fphi[n.nf][n.qn][fnode(n.nf, k)], s[fnode(n.nf, k)], r);
   return r;
 }
+// The basis tables staged in a block's shared memory.  The warp-per-cell
+// kernels index them by lane (point, face, vertex): from constant memory,
+// whose cache serves one address per cycle, those divergent reads would be
+// serialised.
+constexpr int TAB3 = NQ * NN + NQ * NN * 3 + 6 * NF * NN;
+struct Tab3S {
+  const double (*phi)[NN];
+  const double (*dphi)[NN][3];
+  const double (*fphi)[NF][NN];
+};
+__device__ __forceinline__ Tab3S stage_tab3(double *buf) {
+  const double *src[3] = {&c_phi[0][0], &c_dphi[0][0][0], &c_fphi[0][0][0]};
+  const int len[3] = {NQ * NN, NQ * NN * 3, 6 * NF * NN};
+  double *dst = buf;
+#pragma unroll
+  for (int t = 0; t < 3; ++t) {
+    for (int e = threadIdx.x; e < len[t]; e += blockDim.x) dst[e] = src[t][e];
+    dst += len[t];
+  }
+  return Tab3S{reinterpret_cast<const double (*)[NN]>(buf),
+               reinterpret_cast<const double (*)[NN][3]>(buf + NQ * NN),
+               reinterpret_cast<const double (*)[NF][NN]>(buf + NQ * NN * 4)};
+}
+__device__ __forceinline__ double at_qs(const double *t, int q, const Tab3S &T) {
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < NN; ++i) s = fma(T.phi[q][i], t[i], s);
+  return s;
+}
+__device__ __forceinline__ double at_faces(const double *t, int f, int q, const Tab3S &T) {
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) s = fma(T.fphi[f][q][fnode(f, k)], t[fnode(f, k)], s);
+  return s;
+}
+__device__ __forceinline__ double nb_vals(const NbPt &n, const double *v, int ncomp, int comp,
+                                          const Tab3S &T) {
+  const double *s = v + ((long)n.nb * ncomp + comp) * NN;
+  double r = 0.0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) r = fma(T.fphi[n.nf][n.qn][fnode(n.nf, k)], s[fnode(n.nf, k)], r);
+  return r;
+}
 // out[i] += sum_q (V_q phi_i + sum_e Gr_q[e] dphi_i/dxi_e) at the cell points;
 // V and Gr already carry JxW (Gr in reference directions)
 __device__ __forceinline__ void integ(double *out, const double *V, const double (*Gr)[3]) {
@@ -128,15 +171,15 @@ __device__ __forceinline__ void tile3(double *dst, const double *src, int c, int
 // with 32).  Every lane of the warp must call it; lanes 0..7 hold the result
 // of their vertex (all lanes do).
 __device__ __forceinline__ double gather3(const double (*sv)[4], const double (*sf)[NF],
-                                          int lane) {
+                                          int lane, const Tab3S &T) {
   const int i = lane & 7, part = lane >> 3;
   double o = 0.0;
   for (int q = part; q < NQ; q += 4)
-    o += sv[q][0] * c_phi[q][i] + sv[q][1] * c_dphi[q][i][0] + sv[q][2] * c_dphi[q][i][1] +
-         sv[q][3] * c_dphi[q][i][2];
+    o += sv[q][0] * T.phi[q][i] + sv[q][1] * T.dphi[q][i][0] + sv[q][2] * T.dphi[q][i][1] +
+         sv[q][3] * T.dphi[q][i][2];
   for (int t = part; t < 3 * NF; t += 4) {
     const int a = t / NF, q = t - a * NF, f = 2 * a + ((i >> a) & 1);
-    o += sf[f][q] * c_fphi[f][q][i];
+    o += sf[f][q] * T.fphi[f][q][i];
   }
   o += __shfl_xor_sync(0xffffffffu, o, 8);
   o += __shfl_xor_sync(0xffffffffu, o, 16);
@@ -146,15 +189,15 @@ __device__ __forceinline__ double gather3(const double (*sv)[4], const double (*
 // The same sums for vertex i by one lane alone (three components at once
 // keep 24 of the 32 lanes busy without the shuffles)
 __device__ __forceinline__ double gather3_one(const double (*sv)[4], const double (*sf)[NF],
-                                              int i) {
+                                              int i, const Tab3S &T) {
   double o = 0.0;
   for (int q = 0; q < NQ; ++q)
-    o += sv[q][0] * c_phi[q][i] + sv[q][1] * c_dphi[q][i][0] + sv[q][2] * c_dphi[q][i][1] +
-         sv[q][3] * c_dphi[q][i][2];
+    o += sv[q][0] * T.phi[q][i] + sv[q][1] * T.dphi[q][i][0] + sv[q][2] * T.dphi[q][i][1] +
+         sv[q][3] * T.dphi[q][i][2];
   for (int a = 0; a < 3; ++a) {  // the faces holding vertex i, in increasing order
     const int f = 2 * a + ((i >> a) & 1);
 #pragma unroll
-    for (int q = 0; q < NF; ++q) o += sf[f][q] * c_fphi[f][q][i];
+    for (int q = 0; q < NF; ++q) o += sf[f][q] * T.fphi[f][q][i];
   }
   return o;
 }
@@ -168,6 +211,8 @@ __global__ void __launch_bounds__(32 * CELLS3)
   const int lc = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = blockIdx.x * CELLS3 + lc;
   const bool active = c < g.nc;
+  __shared__ double stab[TAB3];
+  const Tab3S T = stage_tab3(stab);  // read after the first barrier
   if (active)
     for (int j = 0; j < co.nst; ++j) {
       tile3(srt[lc][j], src.p[2 * j], c, 1, lane);
@@ -178,11 +223,11 @@ __global__ void __launch_bounds__(32 * CELLS3)
     if (lane < NQ) {
       const int q = lane;
       const double *cq = g.cg + ((long)c * NQ + q) * 13;
-      sv[lc][q][0] = at_q(srt[lc][0], q) * cq[9];
+      sv[lc][q][0] = at_qs(srt[lc][0], q, T) * cq[9];
       double P[3] = {0, 0, 0};
       for (int j = 0; j < co.nst; ++j) {
-        const double r = at_q(srt[lc][j], q), w = co.ca[j] * co.dt * r;
-        for (int d = 0; d < 3; ++d) P[d] += w * at_q(sut[lc][j][d], q);
+        const double r = at_qs(srt[lc][j], q, T), w = co.ca[j] * co.dt * r;
+        for (int d = 0; d < 3; ++d) P[d] += w * at_qs(sut[lc][j][d], q, T);
       }
       to_ref(cq, P, &sv[lc][q][1]);
     }
@@ -194,11 +239,11 @@ __global__ void __launch_bounds__(32 * CELLS3)
         double flux = 0.0;
         const NbPt np = nb_point(g, c, f, q);
         for (int j = 0; j < co.nst; ++j) {
-          const double ro = at_face(srt[lc][j], f, q), rn = nb_val(np, src.p[2 * j], 1, 0);
+          const double ro = at_faces(srt[lc][j], f, q, T), rn = nb_vals(np, src.p[2 * j], 1, 0, T);
           double avg = 0.0, uno = 0.0, unn = 0.0;
           for (int d = 0; d < 3; ++d) {
-            const double uo = at_face(sut[lc][j][d], f, q);
-            const double un = nb_val(np, src.p[2 * j + 1], 3, d);
+            const double uo = at_faces(sut[lc][j][d], f, q, T);
+            const double un = nb_vals(np, src.p[2 * j + 1], 3, d, T);
             avg += 0.5 * (ro * uo + rn * un) * fq[d];
             uno += uo * fq[d];
             unn += un * fq[d];
@@ -212,7 +257,7 @@ __global__ void __launch_bounds__(32 * CELLS3)
   }
   __syncthreads();
   if (active) {  // warp-uniform: every lane of the cell's warp takes part
-    const double o = gather3(sv[lc], sf[lc], lane);
+    const double o = gather3(sv[lc], sf[lc], lane, T);
     if (lane < NN) dst[(long)c * NN + lane] = o;
   }
 }
@@ -228,6 +273,8 @@ __global__ void __launch_bounds__(32 * CELLS3)
   const int lc = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = blockIdx.x * CELLS3 + lc;
   const bool active = c < g.nc;
+  __shared__ double stab[TAB3];
+  const Tab3S T = stage_tab3(stab);  // read after the first barrier
   const double iM2 = 1.0 / (co.Ma * co.Ma), iF2 = 1.0 / (co.Fr * co.Fr);
   if (active) {
     for (int j = 0; j < co.nst; ++j) {
@@ -243,15 +290,15 @@ __global__ void __launch_bounds__(32 * CELLS3)
       const int q = lane;
       const double *cq = g.cg + ((long)c * NQ + q) * 13;
       for (int d = 0; d < 3; ++d) {
-        double v = at_q(srt[lc][0], q) * at_q(sut[lc][0][d], q);
+        double v = at_qs(srt[lc][0], q, T) * at_qs(sut[lc][0][d], q, T);
         for (int j = 0; j < co.ng; ++j)
-          v -= co.cg[j] * co.dt * iF2 * at_q(sgt[lc][j], q) * cq[10 + d];
+          v -= co.cg[j] * co.dt * iF2 * at_qs(sgt[lc][j], q, T) * cq[10 + d];
         sv[lc][d][q][0] = v * cq[9];
         double P[3] = {0, 0, 0};
         for (int j = 0; j < co.nst; ++j) {
-          const double ru = co.ca[j] * co.dt * at_q(srt[lc][j], q) * at_q(sut[lc][j][d], q);
-          for (int k = 0; k < 3; ++k) P[k] += ru * at_q(sut[lc][j][k], q);
-          P[d] += co.ct[j] * co.dt * iM2 * at_q(spt[lc][j], q);
+          const double ru = co.ca[j] * co.dt * at_qs(srt[lc][j], q, T) * at_qs(sut[lc][j][d], q, T);
+          for (int k = 0; k < 3; ++k) P[k] += ru * at_qs(sut[lc][j][k], q, T);
+          P[d] += co.ct[j] * co.dt * iM2 * at_qs(spt[lc][j], q, T);
         }
         to_ref(cq, P, &sv[lc][d][q][1]);  // the geometry factors carry JxW
       }
@@ -263,17 +310,17 @@ __global__ void __launch_bounds__(32 * CELLS3)
       const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
       double fl[3] = {0, 0, 0};
       for (int j = 0; j < co.nst; ++j) {
-        const double po = at_face(spt[lc][j], f, q);
+        const double po = at_faces(spt[lc][j], f, q, T);
         if (wall) {  // p_D = p (euler_operator.h:2189-2305)
           for (int d = 0; d < 3; ++d) fl[d] += co.ct[j] * co.dt * iM2 * 0.5 * (po + po) * fq[d];
           continue;
         }
-        const double ro = at_face(srt[lc][j], f, q), rn = nb_val(np, src.p[3 * j], 1, 0);
-        const double pn = nb_val(np, src.p[3 * j + 2], 1, 0);
+        const double ro = at_faces(srt[lc][j], f, q, T), rn = nb_vals(np, src.p[3 * j], 1, 0, T);
+        const double pn = nb_vals(np, src.p[3 * j + 2], 1, 0, T);
         double uo[3], un[3], uno = 0.0, unn = 0.0;
         for (int k = 0; k < 3; ++k) {
-          uo[k] = at_face(sut[lc][j][k], f, q);
-          un[k] = nb_val(np, src.p[3 * j + 1], 3, k);
+          uo[k] = at_faces(sut[lc][j][k], f, q, T);
+          un[k] = nb_vals(np, src.p[3 * j + 1], 3, k, T);
           uno += uo[k] * fq[k];
           unn += un[k] * fq[k];
         }
@@ -289,7 +336,7 @@ __global__ void __launch_bounds__(32 * CELLS3)
   __syncthreads();
   if (active && lane < 3 * NN) {
     const int d = lane / NN, i = lane - d * NN;
-    dst[((long)c * 3 + d) * NN + i] = gather3_one(sv[lc][d], sf[lc][d], i);
+    dst[((long)c * 3 + d) * NN + i] = gather3_one(sv[lc][d], sf[lc][d], i, T);
   }
 }
 
@@ -310,6 +357,8 @@ __global__ void __launch_bounds__(32 * CELLS3)
   const int lc = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = blockIdx.x * CELLS3 + lc;
   const bool active = c < g.nc;
+  __shared__ double stab[TAB3];
+  const Tab3S T = stage_tab3(stab);  // read after the first barrier
   const double ig = 1.0 / (GAS_GAMMA - 1.0), hgf = GAS_GAMMA / (GAS_GAMMA - 1.0);
   const double M2 = co.Ma * co.Ma, iF2 = 1.0 / (co.Fr * co.Fr);
   if (active) {
@@ -328,32 +377,32 @@ __global__ void __launch_bounds__(32 * CELLS3)
     if (lane < NQ) {
       const int q = lane;
       const double *cq = g.cg + ((long)c * NQ + q) * 13;
-      const double r0 = at_q(srt[lc][0], q), p0 = at_q(spt[lc][0], q);
+      const double r0 = at_qs(srt[lc][0], q, T), p0 = at_qs(spt[lc][0], q, T);
       double uu0 = 0.0;
       for (int d = 0; d < 3; ++d) {
-        const double u = at_q(sut[lc][0][d], q);
+        const double u = at_qs(sut[lc][0][d], q, T);
         uu0 += u * u;
       }
-      const double kr = at_q(sgr[lc][co.ng], q);
+      const double kr = at_qs(sgr[lc][co.ng], q, T);
       double kk = 0.0;
       for (int d = 0; d < 3; ++d) {
-        const double kv = at_q(sgu[lc][co.ng][d], q);
+        const double kv = at_qs(sgu[lc][co.ng][d], q, T);
         kk += kv * kv;
       }
       double v = ig * p0 + 0.5 * M2 * uu0 * r0 - 0.5 * kr * M2 * kk;  // rho E - kinetic
       for (int j = 0; j < co.ng; ++j) {
-        const double gr = at_q(sgr[lc][j], q);
+        const double gr = at_qs(sgr[lc][j], q, T);
         double ue = 0.0;
-        for (int d = 0; d < 3; ++d) ue += at_q(sgu[lc][j][d], q) * cq[10 + d];  // u . e_r a^2/r^2
+        for (int d = 0; d < 3; ++d) ue += at_qs(sgu[lc][j][d], q, T) * cq[10 + d];  // u . e_r a^2/r^2
         v -= co.cg[j] * co.dt * M2 * iF2 * gr * ue;
       }
       sv[lc][q][0] = v * cq[9];
       double P[3] = {0, 0, 0};
       for (int j = 0; j < co.nst; ++j) {
-        const double r = at_q(srt[lc][j], q), p = at_q(spt[lc][j], q);
+        const double r = at_qs(srt[lc][j], q, T), p = at_qs(spt[lc][j], q, T);
         double u[3], uu = 0.0;
         for (int d = 0; d < 3; ++d) {
-          u[d] = at_q(sut[lc][j][d], q);
+          u[d] = at_qs(sut[lc][j][d], q, T);
           uu += u[d] * u[d];
         }
         const double w = 0.5 * co.ca[j] * co.dt * M2 * uu * r + co.ct[j] * co.dt * hgf * p;
@@ -370,13 +419,13 @@ __global__ void __launch_bounds__(32 * CELLS3)
         double uo[3][3], un[3][3];
         for (int j = 0; j < co.nst; ++j)
           for (int d = 0; d < 3; ++d) {
-            uo[j][d] = at_face(sut[lc][j][d], f, q);
-            un[j][d] = nb_val(np, src.p[3 * j + 1], 3, d);
+            uo[j][d] = at_faces(sut[lc][j][d], f, q, T);
+            un[j][d] = nb_vals(np, src.p[3 * j + 1], 3, d, T);
           }
         double flux = 0.0;
         for (int j = 0; j < co.nst; ++j) {
-          const double ro = at_face(srt[lc][j], f, q), rn = nb_val(np, src.p[3 * j], 1, 0);
-          const double po = at_face(spt[lc][j], f, q), pn = nb_val(np, src.p[3 * j + 2], 1, 0);
+          const double ro = at_faces(srt[lc][j], f, q, T), rn = nb_vals(np, src.p[3 * j], 1, 0, T);
+          const double po = at_faces(spt[lc][j], f, q, T), pn = nb_vals(np, src.p[3 * j + 2], 1, 0, T);
           double uuo = 0, uun = 0, uno = 0, unn = 0;
           for (int d = 0; d < 3; ++d) {
             uuo += uo[j][d] * uo[j][d]; uun += un[j][d] * un[j][d];
@@ -410,7 +459,7 @@ __global__ void __launch_bounds__(32 * CELLS3)
   }
   __syncthreads();
   if (active) {  // warp-uniform: every lane of the cell's warp takes part
-    const double o = gather3(sv[lc], sf[lc], lane);
+    const double o = gather3(sv[lc], sf[lc], lane, T);
     if (lane < NN) dst[(long)c * NN + lane] = o;
   }
 }
@@ -427,13 +476,15 @@ __global__ void __launch_bounds__(32 * CELLS3)
   const int lc = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = blockIdx.x * CELLS3 + lc;
   const bool active = c < g.nc;
+  __shared__ double stab[TAB3];
+  const Tab3S T = stage_tab3(stab);  // read after the first barrier
   if (active && lane < NN) sp[lc][lane] = p[(long)c * NN + lane];
   __syncthreads();
   if (active) {
     if (lane < NQ) {
       const int q = lane;
       const double *cq = g.cg + ((long)c * NQ + q) * 13;
-      const double s = -cB * at_q(sp[lc], q);
+      const double s = -cB * at_qs(sp[lc], q, T);
 #pragma unroll
       for (int d = 0; d < 3; ++d)
 #pragma unroll
@@ -442,9 +493,9 @@ __global__ void __launch_bounds__(32 * CELLS3)
     for (int e = lane; e < 6 * NF; e += 32) {
       const int f = e / NF, q = e - f * NF;
       const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
-      const double po = at_face(sp[lc], f, q);
+      const double po = at_faces(sp[lc], f, q, T);
       const NbPt np = nb_point(g, c, f, q);
-      const double pn = np.nb < 0 ? po : nb_val(np, p, 1, 0);
+      const double pn = np.nb < 0 ? po : nb_vals(np, p, 1, 0, T);
       const double a = cB * 0.5 * (po + pn) * fq[3];
 #pragma unroll
       for (int d = 0; d < 3; ++d) sfn[lc][f][q][d] = a * fq[d];
@@ -455,12 +506,12 @@ __global__ void __launch_bounds__(32 * CELLS3)
     const int d = lane / NN, i = lane - d * NN;
     double o = 0.0;
     for (int q = 0; q < NQ; ++q)
-      o += sgr[lc][q][d][0] * c_dphi[q][i][0] + sgr[lc][q][d][1] * c_dphi[q][i][1] +
-           sgr[lc][q][d][2] * c_dphi[q][i][2];
+      o += sgr[lc][q][d][0] * T.dphi[q][i][0] + sgr[lc][q][d][1] * T.dphi[q][i][1] +
+           sgr[lc][q][d][2] * T.dphi[q][i][2];
     for (int a = 0; a < 3; ++a) {  // the faces holding vertex i
       const int f = 2 * a + ((i >> a) & 1);
 #pragma unroll
-      for (int q = 0; q < NF; ++q) o += sfn[lc][f][q][d] * c_fphi[f][q][i];
+      for (int q = 0; q < NF; ++q) o += sfn[lc][f][q][d] * T.fphi[f][q][i];
     }
     sout[lc][d][i] = o;
   }
@@ -493,6 +544,8 @@ __global__ void __launch_bounds__(32 * CELLS3)
   const int lc = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = blockIdx.x * CELLS3 + lc;
   const bool active = c < g.nc;
+  __shared__ double stab[TAB3];
+  const Tab3S T = stage_tab3(stab);  // read after the first barrier
   // 1/(gamma-1) as a constant factor: a division by (gamma-1) at every point
   // would cost an FP64 division sequence each (the values agree to rounding)
   const double hg = GAS_GAMMA / (GAS_GAMMA - 1.0), ig = 1.0 / (GAS_GAMMA - 1.0);
@@ -508,13 +561,13 @@ __global__ void __launch_bounds__(32 * CELLS3)
     if (lane < NQ) {
       const int q = lane;
       const double *cq = g.cg + ((long)c * NQ + q) * 13;
-      const double pf = at_q(sft[lc], q);
+      const double pf = at_qs(sft[lc], q, T);
       double P[3];
 #pragma unroll
-      for (int d = 0; d < 3; ++d) P[d] = sc * (-cC * hg * pf * at_q(swt[lc][d], q));
+      for (int d = 0; d < 3; ++d) P[d] = sc * (-cC * hg * pf * at_qs(swt[lc][d], q, T));
       double Gr[3];
       to_ref(cq, P, Gr);
-      sv[lc][q][0] = withD ? at_q(spt[lc], q) * ig * cq[9] : 0.0;
+      sv[lc][q][0] = withD ? at_qs(spt[lc], q, T) * ig * cq[9] : 0.0;
 #pragma unroll
       for (int e = 0; e < 3; ++e) sv[lc][q][1 + e] = Gr[e];
     }
@@ -524,11 +577,11 @@ __global__ void __launch_bounds__(32 * CELLS3)
       const NbPt np = nb_point(g, c, f, q);
       if (np.nb >= 0) {  // no boundary term
         const double *fq = g.fg + (((long)c * 6 + f) * NF + q) * 4;
-        const double pfo = at_face(sft[lc], f, q), pfn = nb_val(np, pfix, 1, 0);
+        const double pfo = at_faces(sft[lc], f, q, T), pfn = nb_vals(np, pfix, 1, 0, T);
         double av = 0.0, wno = 0.0, wnn = 0.0;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-          const double wo = at_face(swt[lc][d], f, q), wn = nb_val(np, w, 3, d);
+          const double wo = at_faces(swt[lc][d], f, q, T), wn = nb_vals(np, w, 3, d, T);
           av += 0.5 * hg * (pfo * wo + pfn * wn) * fq[d];
           wno += wo * fq[d];
           wnn += wn * fq[d];
@@ -541,7 +594,7 @@ __global__ void __launch_bounds__(32 * CELLS3)
   }
   __syncthreads();
   if (active) {  // warp-uniform: every lane of the cell's warp takes part
-    const double o = gather3(sv[lc], sfa[lc], lane);
+    const double o = gather3(sv[lc], sfa[lc], lane, T);
     if (lane >= NN) return;
     const int i = lane;
     const long gi = (long)c * NN + i;
