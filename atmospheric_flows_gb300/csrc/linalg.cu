@@ -138,6 +138,56 @@ __global__ void k_multiaxpy(double *__restrict__ w, const double *__restrict__ V
   }
 }
 
+// w <- w - sum_l h[l] V_l over all m vectors, then the first M dot products
+// V_l . w with the updated w: "subtract, then project again" of CGS2 in one
+// sweep over V.  The per-element sums, the element-to-thread map and the
+// summation order are those of k_multiaxpy and k_multidot_partial, so the
+// results are the same bits as the two separate kernels.
+template <int M>
+__global__ void k_axpy_multidot(double *__restrict__ w, const double *__restrict__ V, long ldv,
+                                int m, const double *__restrict__ h, long n,
+                                double *__restrict__ red) {
+  __shared__ double sh[RT / 32];
+  double acc[M];
+#pragma unroll
+  for (int l = 0; l < M; ++l) acc[l] = 0.0;
+  for (long i = (long)blockIdx.x * RT + threadIdx.x; i < n; i += (long)RED_BLOCKS * RT) {
+    double v[M], s = 0.0;
+#pragma unroll
+    for (int l = 0; l < M; ++l) {
+      v[l] = V[l * ldv + i];
+      s = fma(h[l], v[l], s);
+    }
+    for (int l = M; l < m; ++l) s = fma(h[l], V[l * ldv + i], s);
+    const double wi = w[i] + -1.0 * s;
+    w[i] = wi;
+#pragma unroll
+    for (int l = 0; l < M; ++l) acc[l] = fma(v[l], wi, acc[l]);
+  }
+#pragma unroll
+  for (int l = 0; l < M; ++l) {
+    const double t = block_reduce<0>(acc[l], sh);
+    if (threadIdx.x == 0) red[(long)l * RED_BLOCKS + blockIdx.x] = t;
+  }
+}
+
+// w <- w - sum_l h[l] V_l, then |w|^2 (k_multiaxpy followed by k_dot_partial
+// on w, in one sweep, same bits)
+__global__ void k_axpy_dot(double *__restrict__ w, const double *__restrict__ V, long ldv, int m,
+                           const double *__restrict__ h, long n, double *__restrict__ red) {
+  __shared__ double sh[RT / 32];
+  double acc = 0.0;
+  for (long i = (long)blockIdx.x * RT + threadIdx.x; i < n; i += (long)RED_BLOCKS * RT) {
+    double s = 0.0;
+    for (int l = 0; l < m; ++l) s = fma(h[l], V[l * ldv + i], s);
+    const double wi = w[i] + -1.0 * s;
+    w[i] = wi;
+    acc = fma(wi, wi, acc);
+  }
+  acc = block_reduce<0>(acc, sh);
+  if (threadIdx.x == 0) red[blockIdx.x] = acc;
+}
+
 __global__ void k_maxdiff_partial(const double *__restrict__ a, const double *__restrict__ b,
                                   long n, double *__restrict__ red) {
   __shared__ double sh[RT / 32];
@@ -260,12 +310,35 @@ int vec_multiaxpy(cudaStream_t st, double *w, const double *V, long ldv, int m,
 int arnoldi_step(cudaStream_t st, double *V, long n, int j, double *w, double *red,
                  double *dsmall, double *h_pinned, double *hcol, double *hn) {
   double *h1 = dsmall, *h2 = dsmall + 32, *nsq = dsmall + 64;
+  const int m = j + 1;
+  if (m > MAXM) return ATM_BAD_ARG;
   int rc;
-  if ((rc = vec_multidot(st, V, n, j + 1, w, n, red, h1))) return rc;
-  if ((rc = vec_multiaxpy(st, w, V, n, j + 1, h1, -1.0, n))) return rc;
-  if ((rc = vec_multidot(st, V, n, j + 1, w, n, red, h2))) return rc;
-  if ((rc = vec_multiaxpy(st, w, V, n, j + 1, h2, -1.0, n))) return rc;
-  if ((rc = vec_dot(st, w, w, n, red, nsq))) return rc;
+  // h1 = V^T w
+  if ((rc = vec_multidot(st, V, n, m, w, n, red, h1))) return rc;
+  // w -= V h1 and h2 = V^T w, fused over the first 8 vectors
+  const int m0 = m < 8 ? m : 8;
+  switch (m0) {
+    case 1: k_axpy_multidot<1><<<RED_BLOCKS, RT, 0, st>>>(w, V, n, m, h1, n, red); break;
+    case 2: k_axpy_multidot<2><<<RED_BLOCKS, RT, 0, st>>>(w, V, n, m, h1, n, red); break;
+    case 3: k_axpy_multidot<3><<<RED_BLOCKS, RT, 0, st>>>(w, V, n, m, h1, n, red); break;
+    case 4: k_axpy_multidot<4><<<RED_BLOCKS, RT, 0, st>>>(w, V, n, m, h1, n, red); break;
+    case 5: k_axpy_multidot<5><<<RED_BLOCKS, RT, 0, st>>>(w, V, n, m, h1, n, red); break;
+    case 6: k_axpy_multidot<6><<<RED_BLOCKS, RT, 0, st>>>(w, V, n, m, h1, n, red); break;
+    case 7: k_axpy_multidot<7><<<RED_BLOCKS, RT, 0, st>>>(w, V, n, m, h1, n, red); break;
+    default: k_axpy_multidot<8><<<RED_BLOCKS, RT, 0, st>>>(w, V, n, m, h1, n, red); break;
+  }
+  g_kernel_launches.fetch_add(1);
+  for (int l0 = 8; l0 < m; l0 += 8) {
+    const int mm = m - l0 < 8 ? m - l0 : 8;
+    multidot_chunk(st, V + (long)l0 * n, n, mm, w, n, red + (long)l0 * RED_BLOCKS);
+  }
+  k_finalize<0><<<m, RT, 0, st>>>(red, h2);
+  ATM_CHECK_LAUNCH("k_axpy_multidot");
+  // w -= V h2 and |w|^2
+  k_axpy_dot<<<RED_BLOCKS, RT, 0, st>>>(w, V, n, m, h2, n, red);
+  g_kernel_launches.fetch_add(1);
+  k_finalize<0><<<1, RT, 0, st>>>(red, nsq);
+  ATM_CHECK_LAUNCH("k_axpy_dot");
   ATM_CUDA(cudaMemcpyAsync(h_pinned, dsmall, 65 * sizeof(double), cudaMemcpyDeviceToHost, st));
   ATM_CUDA(cudaStreamSynchronize(st));
   for (int l = 0; l <= j; ++l) hcol[l] = h_pinned[l] + h_pinned[32 + l];

@@ -175,7 +175,7 @@ class EULEROperator:
                   self.storage.mapping_degree, pn, len(inner), pi, len(bdry), pb, pc)
 
     def set_mg_smoother(self, degree=4, smoothing_range=15.0, eig_iterations=10,
-                        coarse_degree=10):
+                        coarse_degree=6):
         _lib.call("atm_mg_set_smoother", self._h, int(degree), float(smoothing_range),
                   int(eig_iterations), int(coarse_degree))
 

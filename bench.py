@@ -92,7 +92,7 @@ def parse():
     ap.add_argument("--vcycle-no-graphs", action="store_true")
     ap.add_argument("--vcycle-fp64", action="store_true")
     ap.add_argument("--mg-levels", type=int, default=3)
-    ap.add_argument("--mg-coarse-degree", type=int, default=10)
+    ap.add_argument("--mg-coarse-degree", type=int, default=6)
     ap.add_argument("--mg-smoother-degree", type=int, default=4)
     ap.add_argument("--shell", action="store_true",
                     help="time IMEX steps of the 3D spherical shell (the reference's own case, "

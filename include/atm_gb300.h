@@ -204,7 +204,7 @@ int atm_mg_add_level(atm_handle h, int n_cells, int mapping_degree, const double
                      const int *children);
 /* Chebyshev degree (4; the reference's 3 needs more FGMRES iterations),
  * smoothing range (15), power iterations for the largest eigenvalue (10),
- * degree of the coarsest-level Chebyshev (10).  Replaces the smoother_data
+ * degree of the coarsest-level Chebyshev (6).  Replaces the smoother_data
  * set-up of Atmospheric_Flow.cc:477-498,594-615. */
 int atm_mg_set_smoother(atm_handle h, int degree, double smoothing_range, int eig_iterations,
                         int coarse_degree);
