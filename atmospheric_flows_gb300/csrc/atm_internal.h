@@ -223,7 +223,9 @@ int vec_dot(cudaStream_t st, const double *x, const double *y, long n, double *r
 // One Arnoldi orthogonalisation of the new direction w against V_0..V_j,
 // all of length n with stride n: classical Gram-Schmidt with one
 // re-orthogonalisation pass (CGS2), then V_{j+1} = w / |w| when |w| is
-// nonzero (w is overwritten by the unscaled result).  hcol[0..j] gets the projection
+// nonzero (w is overwritten by the unscaled result), in three sweeps over V:
+// project; subtract and project again; subtract and take the norm (the
+// arithmetic of five separate kernels, the same bits).  hcol[0..j] gets the projection
 // coefficients, *hn the remaining norm.  `dsmall` is device scratch of >= 65
 // values (dsmall[64] ends as |V_{j+1}|^2 before the scaling), `h_pinned` a
 // pinned host mirror of >= 65; one stream synchronisation.  (A second pass

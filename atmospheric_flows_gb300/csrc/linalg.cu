@@ -311,7 +311,10 @@ int arnoldi_step(cudaStream_t st, double *V, long n, int j, double *w, double *r
                  double *dsmall, double *h_pinned, double *hcol, double *hn) {
   double *h1 = dsmall, *h2 = dsmall + 32, *nsq = dsmall + 64;
   const int m = j + 1;
-  if (m > MAXM) return ATM_BAD_ARG;
+  if (m > MAXM) {
+    set_error("Arnoldi step: more basis vectors than the reduction buffer holds");
+    return ATM_BAD_ARG;
+  }
   int rc;
   // h1 = V^T w
   if ((rc = vec_multidot(st, V, n, m, w, n, red, h1))) return rc;
