@@ -449,8 +449,16 @@ def run_gb300(args):
         _lib.call("atm_solver_get_state", h, *ptrs)
     barrier()
     e2e_s = group.max(time.perf_counter() - t0)
+    # the copies alone (upload and read-back of one state), for the record
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _lib.call("atm_solver_set_state", h, *ptrs)
+        _lib.call("atm_solver_get_state", h, *ptrs)
+    copy_s = time.perf_counter() - t0
     e2e = {"value": ws * case.n_dofs * args.steps / e2e_s, "unit": UNIT,
-           "h2d_bytes_per_step": int(8 * 4 * ns), "d2h_bytes_per_step": int(8 * 4 * ns)}
+           "h2d_bytes_per_step": int(8 * 4 * ns), "d2h_bytes_per_step": int(8 * 4 * ns),
+           "ms_per_step": e2e_s * 1e3 / args.steps,
+           "copy_ms_per_step": copy_s * 1e3 / args.steps}
     solver.close()
     variants = {}
     if not args.only_headline:
