@@ -67,12 +67,6 @@ __device__ __forceinline__ int fnode(int f, int k) {
   const int a = f >> 1, lo = k & ((1 << a) - 1);
   return lo | ((f & 1) << a) | ((k >> a) << (a + 1));
 }
-__device__ __forceinline__ double at_face(const double *t, int f, int q) {
-  double s = 0.0;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) s = fma(c_fphi[f][q][fnode(f, k)], t[fnode(f, k)], s);
-  return s;
-}
 // the neighbour across face f of cell c at own face point q: its cell, its
 // local face and the matching point there (loaded once per face point)
 struct NbPt {
@@ -80,14 +74,6 @@ struct NbPt {
 };
 __device__ __forceinline__ NbPt nb_point(const Geo3 &g, int c, int f, int q) {
   return NbPt{g.nbr[c * 6 + f], g.nbf[c * 6 + f], g.nperm[(c * 6 + f) * NF + q]};
-}
-// the neighbour's trace of component comp of a field with ncomp components
-__device__ __forceinline__ double nb_val(const NbPt &n, const double *v, int ncomp, int comp) {
-  const double *s = v + ((long)n.nb * ncomp + comp) * NN;
-  double r = 0.0;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) r = fma(c_fphi[n.nf][n.qn][fnode(n.nf, k)], s[fnode(n.nf, k)], r);
-  return r;
 }
 // The basis tables staged in a block's shared memory.  The warp-per-cell
 // kernels index them by lane (point, face, vertex): from constant memory,
@@ -112,18 +98,21 @@ __device__ __forceinline__ Tab3S stage_tab3(double *buf) {
                reinterpret_cast<const double (*)[NN][3]>(buf + NQ * NN),
                reinterpret_cast<const double (*)[NF][NN]>(buf + NQ * NN * 4)};
 }
+// value of the vertex field t at cell point q
 __device__ __forceinline__ double at_qs(const double *t, int q, const Tab3S &T) {
   double s = 0.0;
 #pragma unroll
   for (int i = 0; i < NN; ++i) s = fma(T.phi[q][i], t[i], s);
   return s;
 }
+// trace of t at point q of local face f (the face's four vertices)
 __device__ __forceinline__ double at_faces(const double *t, int f, int q, const Tab3S &T) {
   double s = 0.0;
 #pragma unroll
   for (int k = 0; k < 4; ++k) s = fma(T.fphi[f][q][fnode(f, k)], t[fnode(f, k)], s);
   return s;
 }
+// the neighbour's trace of component comp of a field with ncomp components
 __device__ __forceinline__ double nb_vals(const NbPt &n, const double *v, int ncomp, int comp,
                                           const Tab3S &T) {
   const double *s = v + ((long)n.nb * ncomp + comp) * NN;
@@ -131,17 +120,6 @@ __device__ __forceinline__ double nb_vals(const NbPt &n, const double *v, int nc
 #pragma unroll
   for (int k = 0; k < 4; ++k) r = fma(T.fphi[n.nf][n.qn][fnode(n.nf, k)], s[fnode(n.nf, k)], r);
   return r;
-}
-// out[i] += sum_q (V_q phi_i + sum_e Gr_q[e] dphi_i/dxi_e) at the cell points;
-// V and Gr already carry JxW (Gr in reference directions)
-__device__ __forceinline__ void integ(double *out, const double *V, const double (*Gr)[3]) {
-  for (int q = 0; q < NQ; ++q)
-#pragma unroll
-    for (int i = 0; i < NN; ++i) {
-      double s = V ? V[q] * c_phi[q][i] : 0.0;
-      if (Gr) s += Gr[q][0] * c_dphi[q][i][0] + Gr[q][1] * c_dphi[q][i][1] + Gr[q][2] * c_dphi[q][i][2];
-      out[i] += s;
-    }
 }
 // physical vector P (x JxW already) -> reference components Gr[e] = sum_i G[e][i] P_i
 __device__ __forceinline__ void to_ref(const double *cgq, const double *P, double *Gr) {
