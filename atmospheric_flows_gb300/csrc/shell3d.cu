@@ -480,18 +480,22 @@ __global__ void __launch_bounds__(32 * CELLS3)
     }
   }
   __syncthreads();
-  if (active && lane < 3 * NN) {
-    const int d = lane / NN, i = lane - d * NN;
-    double o = 0.0;
-    for (int q = 0; q < NQ; ++q)
-      o += sgr[lc][q][d][0] * T.dphi[q][i][0] + sgr[lc][q][d][1] * T.dphi[q][i][1] +
-           sgr[lc][q][d][2] * T.dphi[q][i][2];
-    for (int a = 0; a < 3; ++a) {  // the faces holding vertex i
-      const int f = 2 * a + ((i >> a) & 1);
+  if (active) {  // warp-uniform; per component, four lanes per vertex (as gather3)
+    const int i = lane & 7, part = lane >> 3;
 #pragma unroll
-      for (int q = 0; q < NF; ++q) o += sfn[lc][f][q][d] * T.fphi[f][q][i];
+    for (int d = 0; d < 3; ++d) {
+      double o = 0.0;
+      for (int q = part; q < NQ; q += 4)
+        o += sgr[lc][q][d][0] * T.dphi[q][i][0] + sgr[lc][q][d][1] * T.dphi[q][i][1] +
+             sgr[lc][q][d][2] * T.dphi[q][i][2];
+      for (int t = part; t < 3 * NF; t += 4) {  // the faces holding vertex i
+        const int a = t / NF, q = t - a * NF, f = 2 * a + ((i >> a) & 1);
+        o += sfn[lc][f][q][d] * T.fphi[f][q][i];
+      }
+      o += __shfl_xor_sync(0xffffffffu, o, 8);
+      o += __shfl_xor_sync(0xffffffffu, o, 16);
+      if (lane < NN) sout[lc][d][i] = o;
     }
-    sout[lc][d][i] = o;
   }
   __syncthreads();
   if (active && lane < 3 * NN) {
